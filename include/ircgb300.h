@@ -1,0 +1,139 @@
+/*
+ * ircgb300.h -- C ABI of the GB300 (sm_103a) IronClust clustering hot path.
+ *
+ * The library replaces the five CUDA kernels IronClust's MATLAB host launches
+ * through parallel.gpu.CUDAKernel + feval, keeping their argument order,
+ * array shapes and outputs, and adds fused per-site entry points that run a
+ * whole site (every drift chunk) per call.
+ *
+ * Conventions (identical to the reference):
+ *   - feature matrices are MATLAB column-major [nC x n] float32, i.e. the nC
+ *     features of one spike are contiguous;
+ *   - 2-D outputs are column-major ([nT x nA] means element (t, a) at
+ *     t + nT*a);
+ *   - returned spike indices are 1-based;
+ *   - SINGLE_INF = (float)3.402E+38 marks "no candidate".
+ * All array arguments are DEVICE pointers unless a comment says "host".
+ * vnConst arrays are read on the host (MATLAB builds them on the host before
+ * uploading them as gpuArrays; the MEX gateway passes the host copy).
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  Every call is
+ * asynchronous with respect to the host and returns IRC_OK or a negative
+ * IRC_E* status; irc_last_error() describes the last failure of the calling
+ * thread.  Kernels never trap: a failed call leaves the context usable.
+ */
+#ifndef IRCGB300_H
+#define IRCGB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define IRC_OK 0
+#define IRC_E_INVAL (-1)   /* bad pointer, size or argument combination   */
+#define IRC_E_NC (-2)      /* feature count above the kernel's maximum      */
+#define IRC_E_CUDA (-3)    /* a CUDA runtime call or launch failed          */
+#define IRC_E_NOMEM (-4)   /* device allocation failed                      */
+#define IRC_E_TIMEOUT (-5) /* a bounded device-side wait gave up            */
+#define IRC_E_UNSUPPORTED (-6) /* mode not available on this device        */
+
+/* precision / search modes of the kNN entry points */
+#define IRC_MODE_REF 0   /* bit-exact with the reference binned-minimum kernels */
+#define IRC_MODE_EXACT 1 /* true top-k, reference FP32 arithmetic, (d2, index) ties */
+#define IRC_MODE_BF16 2  /* tcgen05 BF16 distance filter + exact FP32 re-rank   */
+#define IRC_MODE_FP8 3   /* tcgen05 FP8-e4m3 filter (per-chunk scale) + re-rank */
+
+int irc_version(void);                 /* 10000*major + 100*minor + patch */
+const char *irc_last_error(void);      /* message of the calling thread's last failure */
+const char *irc_status_string(int status);
+
+/* ---------------------------------------------------------------------------
+ * Drop-in kernels (one call == one MATLAB feval of the reference kernel).
+ * Output arrays are fully written (the reference relies on pre-zeroed
+ * outputs only for entries it does not write; these write every entry).
+ * ------------------------------------------------------------------------ */
+
+/* Replaces search_min_drift (matlab/search_min_drift.cu:24; launched from
+ * matlab/irc2.m:3793).  vnConst (host) = {nC, nF, nBB, iA0, nA}.
+ * D, I: [nThreads x nA].  IBB/NBB: [nBB] 0-based run starts / run lengths.
+ * mode IRC_MODE_REF: per-thread-bin minima exactly as the reference.
+ * mode IRC_MODE_EXACT: rows 0..knn-1 hold the true k nearest (distance > 0)
+ * in ascending (distance, index) order, the remaining rows hold
+ * sqrt(SINGLE_INF) and the query's own index, so the unchanged MATLAB
+ * post-processing (sort, first knn rows) returns the exact kNN. */
+int irc_search_min_drift(float *D, int32_t *I, const float *F, const int32_t *IBB,
+                         const int32_t *NBB, const int32_t *vnConst, int nThreads,
+                         int mode, int knn, void *stream);
+
+/* Replaces search_delta_drift (matlab/search_delta_drift.cu:24; launched
+ * from matlab/irc2.m:3846).  R: [nF] rho.  D, I: [nThreads x nA]. */
+int irc_search_delta_drift(float *D, int32_t *I, const float *F, const float *R,
+                           const int32_t *IBB, const int32_t *NBB, const int32_t *vnConst,
+                           int nThreads, void *stream);
+
+/* Replaces cuda_knn_index (matlab/cuda_knn_index.cu:27; launched from
+ * matlab/irc.m:24389).  vnConst (host) = {nB, nA, nC, knn}.  B: [nC x nB],
+ * A: [nC x nA].  K: [nA], I: [knn x nA].  nThreads = the reference block
+ * size (512). */
+int irc_cuda_knn_index(float *K, int32_t *I, const float *B, const float *A,
+                       const int32_t *vnConst, int nThreads, void *stream);
+
+/* Replaces cuda_delta_knn (matlab/cuda_delta_knn.cu:19; launched from
+ * matlab/irc.m:24541).  vnConst (host) = {nB, nA, nC}.  D: [nA], N: [nA]
+ * (1-based into B; falls back to the query's own A-space index, as the
+ * reference does).  nThreads = the reference block size (128). */
+int irc_cuda_delta_knn(float *D, uint32_t *N, const float *B, const float *A,
+                       const float *R_B, const float *R_A, const int32_t *vnConst,
+                       int nThreads, void *stream);
+
+/* Replaces jrc3_cuda_rho_drift (matlab/irc_cuda_rho_drift.cu:28; launched
+ * from matlab/irc.m:24635).  vnConst (host) = {n1, n12, nC}.  miSite12:
+ * [n12 x 2] int32 (primary, secondary site), mrFet1/mrFet2: [nC x n12].
+ * vrRho1: [n1]. */
+int irc_rho_drift(float *vrRho1, const int32_t *miSite12, const float *mrFet1,
+                  const float *mrFet2, const int32_t *vnConst, float dc2, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Fused per-site path.  A plan describes every launch the MATLAB chunk loop
+ * of search_knn_drift_ / search_delta_drift_ (matlab/irc2.m:3764-3788,
+ * :3829-3864) would make for one site: query chunk i covers queries
+ * [q0[i], q0[i]+nq[i]) of the site feature matrix (0-based) and candidate
+ * runs rs[roff[i] .. roff[i+1]-1] / rn[...] (the IBB/NBB of that launch).
+ * Outputs are indexed by q - q_base (n_out entries).  Plan arrays are host
+ * pointers; the plan keeps device copies until irc_plan_destroy.
+ * ------------------------------------------------------------------------ */
+typedef struct irc_plan irc_plan;
+
+int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                    const int32_t *rs, const int32_t *rn, int nChunks, int q_base, int n_out,
+                    int nF);
+int irc_plan_destroy(irc_plan *plan);
+
+/* kNN + rho of every query of the plan (rho_paged_site_ up to the global-id
+ * mapping, matlab/irc2.m:3645-3670).
+ * vrKnn [n_out]: distance of the knn-th neighbour; rho [n_out] (optional) =
+ * 1 ./ vrKnn; miKnn [knn x n_out]: 1-based indices into F; d2Knn
+ * [knn x n_out] (optional, not in REF mode): squared distances.
+ * REF mode = search_min_drift with nThreads bins + MATLAB sort, bit-exact. */
+int irc_site_knn(irc_plan *plan, const float *F, int nC, int knn, int nThreads, int mode,
+                 float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, void *stream);
+
+/* delta + nearest higher-rho neighbour of every query of the plan
+ * (delta_paged_site_ up to the global-id mapping, matlab/irc2.m:3697-3720).
+ * R: [nF] rho of every column of F.  Outputs delta [n_out] =
+ * (distance to the nearest higher-rho spike) .* R(query), nneigh [n_out]
+ * (1-based into F).
+ * REF mode = search_delta_drift with nThreads bins + MATLAB min, bit-exact.
+ * Other modes need miKnn/d2Knn of irc_site_knn (same plan and mode): delta
+ * comes from the kNN list when it holds a higher-rho spike, else from a full
+ * drift-window scan; ties are broken by (distance, index). */
+int irc_site_delta(irc_plan *plan, const float *F, int nC, const float *R, int nThreads,
+                   int mode, int knn, const int32_t *miKnn, const float *d2Knn,
+                   float *delta, int32_t *nneigh, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IRCGB300_H */

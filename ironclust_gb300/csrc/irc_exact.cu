@@ -1,0 +1,376 @@
+// irc_exact.cu -- EXACT-mode site kNN and the kNN-list delta.
+//
+// EXACT kNN: the true k nearest candidates (squared distance > 0, the irc2
+// GPU convention) under the reference FP32 arithmetic, ordered by the key
+// (d2 bits, index).  Two passes per query tile:
+//   1. every thread keeps the minimum over a disjoint stripe of the linked
+//      candidates (256 stripes); the k-th smallest stripe minimum tau bounds
+//      the k-th neighbour distance from above (k distinct candidates lie at
+//      or below it);
+//   2. the stripes are rescanned and candidates with d2 <= tau are appended
+//      to a per-query shared-memory list, which one warp sorts with a
+//      bitonic network; the first k are the answer.
+// A query whose list overflows (mass ties) is finished by a bounded
+// fallback: k ordered scans, each taking the smallest key above the last.
+//
+// kNN-list delta: with the exact kNN list of every spike and rho for all of
+// them, the nearest higher-rho spike is the first list entry whose rho
+// exceeds the query's, whenever the list holds one (any closer higher-rho
+// spike would rank earlier in the list).  Queries without one -- local
+// density peaks -- go to a drift-window scan over all linked candidates.
+#include <cstdio>
+
+#include "irc_common.cuh"
+#include "irc_plan.cuh"
+#include "irc_scan.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;     // = number of stripes
+constexpr int kQB = 16;           // queries per CTA
+constexpr int kCap = 256;         // list capacity per query
+constexpr float kInfSentinel = IRC_SINGLE_INF_F;
+constexpr int kQueueBlocks = 152 * 4;   // grid of the queue-draining kernels (8 warps per block)
+
+__device__ __forceinline__ unsigned long long dkey(float d2, int idx)
+{
+    return ((unsigned long long)__float_as_uint(d2) << 32) | (unsigned)idx;
+}
+
+// Distance of candidate iB to QB staged queries (reference arithmetic).
+template <int QB>
+__device__ __forceinline__ void dist_qb(const float *__restrict__ fb, int nC, const float *sA,
+                                        float (&acc)[QB])
+{
+#pragma unroll
+    for (int q = 0; q < QB; ++q) acc[q] = 0.0f;
+    for (int c = 0; c < nC; ++c) {
+        const float bv = __ldg(fb + c);
+        const float4 *a4 = reinterpret_cast<const float4 *>(sA + c * QB);
+#pragma unroll
+        for (int j = 0; j < QB / 4; ++j) {
+            const float4 a = a4[j];
+            acc[4 * j + 0] = irc::dterm(acc[4 * j + 0], bv, a.x);
+            acc[4 * j + 1] = irc::dterm(acc[4 * j + 1], bv, a.y);
+            acc[4 * j + 2] = irc::dterm(acc[4 * j + 2], bv, a.z);
+            acc[4 * j + 3] = irc::dterm(acc[4 * j + 3], bv, a.w);
+        }
+    }
+}
+
+// Walk this thread's stripe (list positions p = t, t+256, ...) of the
+// concatenated runs r0..r1-1, calling f(candidate index).
+template <class Fn>
+__device__ __forceinline__ void walk_stripe(const irc::PlanDev &p, int r0, int r1, int t, Fn f)
+{
+    int pos = 0;                                   // list position of the run start
+    for (int r = r0; r < r1; ++r) {
+        const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
+        int first = (t - pos) % kThreads;
+        if (first < 0) first += kThreads;
+        for (int i = first; i < rn; i += kThreads) f(rs + i);
+        pos += rn;
+    }
+}
+
+// Warp-wide ascending bitonic sort of kCap 64-bit keys in shared memory.
+__device__ __forceinline__ void warp_sort_keys(unsigned long long *keys, int lane)
+{
+    constexpr int PER = kCap / 32;
+    unsigned long long v[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) v[i] = keys[lane * PER + i];   // element id = lane*PER + i
+    // bitonic over element ids e in [0, kCap)
+#pragma unroll
+    for (int size = 2; size <= kCap; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= PER) {
+                const int lstride = stride / PER;
+#pragma unroll
+                for (int i = 0; i < PER; ++i) {
+                    const int e = lane * PER + i;
+                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, v[i], lstride);
+                    const bool up = ((e & size) == 0);
+                    const bool lower = ((e & stride) == 0);
+                    const bool keep_min = (lower == up);
+                    v[i] = keep_min ? (o < v[i] ? o : v[i]) : (o > v[i] ? o : v[i]);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < PER; ++i) {
+                    const int j = i ^ stride;
+                    if (j > i) {
+                        const int e = lane * PER + i;
+                        const bool up = ((e & size) == 0);
+                        const unsigned long long a = v[i], b = v[j];
+                        const bool swap = up ? (a > b) : (a < b);
+                        v[i] = swap ? b : a;
+                        v[j] = swap ? a : b;
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i) keys[lane * PER + i] = v[i];
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_site_knn_exact(irc::PlanDev p, const float *__restrict__ F, int nC, int knn,
+                 float *__restrict__ vrKnn, float *__restrict__ rho, int *__restrict__ miKnn,
+                 float *__restrict__ d2Knn, int *__restrict__ ovf_count, int *__restrict__ ovf_list)
+{
+    __shared__ __align__(16) float sA[IRC_NC_MAX * kQB];
+    __shared__ float sTau[kQB];
+    __shared__ int sCnt[kQB];
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *sList = reinterpret_cast<unsigned long long *>(dyn);   // [kQB][kCap]
+    float *sMin = reinterpret_cast<float *>(sList + kQB * kCap);              // [kQB][kThreads]
+    int chunk, qs, n;
+    irc::tile_lookup<kQB>(p, blockIdx.x, chunk, qs, n);
+    const int r0 = __ldg(p.roff + chunk), r1 = __ldg(p.roff + chunk + 1);
+    irc::stage_queries<kQB>(F, nC, qs, n, sA);
+    if (threadIdx.x < kQB) sCnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int t = threadIdx.x;
+    // pass 1: stripe minima
+    float mn[kQB];
+#pragma unroll
+    for (int q = 0; q < kQB; ++q) mn[q] = __int_as_float(0x7f800000);
+    walk_stripe(p, r0, r1, t, [&](int iB) {
+        float acc[kQB];
+        dist_qb<kQB>(F + (size_t)iB * nC, nC, sA, acc);
+#pragma unroll
+        for (int q = 0; q < kQB; ++q)
+            if (acc[q] > 0.0f && acc[q] < mn[q]) mn[q] = acc[q];
+    });
+#pragma unroll
+    for (int q = 0; q < kQB; ++q) sMin[q * kThreads + t] = mn[q];
+    __syncthreads();
+    // tau = k-th smallest stripe minimum (by value); +inf if fewer than k finite
+    const int lane = t & 31, warp = t >> 5, nw = kThreads / 32;
+    for (int q = warp; q < kQB; q += nw) {
+        float *m = sMin + q * kThreads;
+        float kth = __int_as_float(0x7f800000);
+        for (int k = 0; k < knn; ++k) {
+            unsigned long long best = ~0ull;
+            for (int s = lane; s < kThreads; s += 32) {
+                const unsigned long long key = dkey(m[s], s);
+                best = key < best ? key : best;
+            }
+            best = irc::warp_min_u64(best);
+            const int s = (int)(best & 0xffffffffu);
+            kth = __uint_as_float((unsigned)(best >> 32));
+            __syncwarp();
+            if (lane == 0) m[s] = __int_as_float(0x7fffffff);      // NaN bits: sorts last
+            __syncwarp();
+            if (!(kth < __int_as_float(0x7f800000))) break;
+        }
+        if (lane == 0) sTau[q] = kth;
+    }
+    __syncthreads();
+    // pass 2: collect d2 <= tau
+    walk_stripe(p, r0, r1, t, [&](int iB) {
+        float acc[kQB];
+        dist_qb<kQB>(F + (size_t)iB * nC, nC, sA, acc);
+#pragma unroll
+        for (int q = 0; q < kQB; ++q)
+            if (acc[q] > 0.0f && acc[q] <= sTau[q]) {
+                const int slot = atomicAdd(&sCnt[q], 1);
+                if (slot < kCap) sList[q * kCap + slot] = dkey(acc[q], iB);
+            }
+    });
+    __syncthreads();
+    for (int q = warp; q < n; q += nw) {
+        const int cnt = sCnt[q];
+        const size_t o = (size_t)(qs + q - p.q_base);
+        if (cnt > kCap) {                          // overflow: finished by the fallback kernel
+            if (lane == 0) { int i = atomicAdd(ovf_count, 1); ovf_list[i] = qs + q; }
+            continue;
+        }
+        unsigned long long *L = sList + q * kCap;
+        for (int i = cnt + lane; i < kCap; i += 32) L[i] = ~0ull;
+        __syncwarp();
+        warp_sort_keys(L, lane);
+        __syncwarp();
+        for (int k = lane; k < knn; k += 32) {
+            const unsigned long long key = L[k];
+            const bool ok = k < cnt;
+            const float d2 = ok ? __uint_as_float((unsigned)(key >> 32)) : kInfSentinel;
+            const int idx = ok ? (int)(key & 0xffffffffu) : qs + q;
+            miKnn[(size_t)k + (size_t)knn * o] = idx + 1;
+            if (d2Knn) d2Knn[(size_t)k + (size_t)knn * o] = d2;
+            if (k == knn - 1) {
+                const float v = irc::ref_sqrt_abs(d2);
+                vrKnn[o] = v;
+                if (rho) rho[o] = __fdiv_rn(1.0f, v);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Warp per overflowing query: k ordered scans, each the smallest key above
+// the previous one.
+__global__ void k_exact_overflow(irc::PlanDev p, const float *__restrict__ F, int nC, int knn,
+                                 const int *__restrict__ ovf_count, const int *__restrict__ ovf_list,
+                                 float *__restrict__ vrKnn, float *__restrict__ rho,
+                                 int *__restrict__ miKnn, float *__restrict__ d2Knn)
+{
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < *ovf_count; w += nwarps) {
+    const int q = ovf_list[w];
+    int lo = 0, hi = p.nChunks;
+    while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (__ldg(p.q0 + mid) <= q) lo = mid; else hi = mid; }
+    const int r0 = __ldg(p.roff + lo), r1 = __ldg(p.roff + lo + 1);
+    const float *a = F + (size_t)q * nC;
+    const size_t o = (size_t)(q - p.q_base);
+    unsigned long long prev = 0;
+    bool have_prev = false;
+    for (int k = 0; k < knn; ++k) {
+        unsigned long long best = ~0ull;
+        for (int r = r0; r < r1; ++r) {
+            const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
+            for (int i = lane; i < rn; i += 32) {
+                const float *b = F + (size_t)(rs + i) * nC;
+                float acc = 0.0f;
+                for (int c = 0; c < nC; ++c) acc = irc::dterm(acc, __ldg(b + c), __ldg(a + c));
+                if (!(acc > 0.0f)) continue;
+                const unsigned long long key = dkey(acc, rs + i);
+                if ((!have_prev || key > prev) && key < best) best = key;
+            }
+        }
+        best = irc::warp_min_u64(best);
+        const bool ok = best != ~0ull;
+        const float d2 = ok ? __uint_as_float((unsigned)(best >> 32)) : kInfSentinel;
+        const int idx = ok ? (int)(best & 0xffffffffu) : q;
+        if (lane == 0) {
+            miKnn[(size_t)k + (size_t)knn * o] = idx + 1;
+            if (d2Knn) d2Knn[(size_t)k + (size_t)knn * o] = d2;
+            if (k == knn - 1) {
+                const float v = irc::ref_sqrt_abs(d2);
+                vrKnn[o] = v;
+                if (rho) rho[o] = __fdiv_rn(1.0f, v);
+            }
+        }
+        if (ok) { prev = best; have_prev = true; }
+    }
+    }
+}
+
+// delta from the kNN list; queries without a higher-rho list entry are queued.
+__global__ void k_delta_list(irc::PlanDev p, const float *__restrict__ R, int knn,
+                             const int *__restrict__ miKnn, const float *__restrict__ d2Knn,
+                             float *__restrict__ delta, int *__restrict__ nneigh,
+                             int *__restrict__ fb_count, int *__restrict__ fb_list)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= p.n_out) return;
+    const int q = o + p.q_base;
+    const float rq = __ldg(R + q);
+    const int *mi = miKnn + (size_t)knn * o;
+    const float *dk = d2Knn + (size_t)knn * o;
+    for (int k = 0; k < knn; ++k) {
+        const float d2 = __ldg(dk + k);
+        if (!(d2 < kInfSentinel)) break;                 // list exhausted
+        const int j = __ldg(mi + k) - 1;
+        if (!(__ldg(R + j) <= rq)) {                     // reference mask: rb <= ra is excluded
+            delta[o] = __fmul_rn(irc::ref_sqrt_abs(d2), rq);
+            nneigh[o] = j + 1;
+            return;
+        }
+    }
+    const int i = atomicAdd(fb_count, 1);
+    fb_list[i] = q;
+}
+
+// Drift-window fallback: warp per queued query, all linked candidates.
+__global__ void k_delta_scan(irc::PlanDev p, const float *__restrict__ F, const float *__restrict__ R,
+                             int nC, const int *__restrict__ fb_count, const int *__restrict__ fb_list,
+                             float *__restrict__ delta, int *__restrict__ nneigh)
+{
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < *fb_count; w += nwarps) {
+    const int q = fb_list[w];
+    int lo = 0, hi = p.nChunks;
+    while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (__ldg(p.q0 + mid) <= q) lo = mid; else hi = mid; }
+    const int r0 = __ldg(p.roff + lo), r1 = __ldg(p.roff + lo + 1);
+    const float *a = F + (size_t)q * nC;
+    const float rq = __ldg(R + q);
+    unsigned long long best = ~0ull;
+    for (int r = r0; r < r1; ++r) {
+        const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
+        for (int i = lane; i < rn; i += 32) {
+            if (__ldg(R + rs + i) <= rq) continue;
+            const float *b = F + (size_t)(rs + i) * nC;
+            float acc = 0.0f;
+            for (int c = 0; c < nC; ++c) acc = irc::dterm(acc, __ldg(b + c), __ldg(a + c));
+            if (!(acc > 0.0f) || !(acc < kInfSentinel)) continue;
+            const unsigned long long key = dkey(acc, rs + i);
+            best = key < best ? key : best;
+        }
+    }
+    best = irc::warp_min_u64(best);
+    if (lane == 0) {
+        const size_t o = (size_t)(q - p.q_base);
+        const bool ok = best != ~0ull;
+        const float d2 = ok ? __uint_as_float((unsigned)(best >> 32)) : kInfSentinel;
+        delta[o] = __fmul_rn(irc::ref_sqrt_abs(d2), rq);
+        nneigh[o] = (ok ? (int)(best & 0xffffffffu) : q) + 1;
+    }
+    }
+}
+
+}  // namespace
+
+// Plan-owned scratch: two counters and two query lists of n_out entries.
+static int irc_plan_scratch(irc_plan *pl, int **counters, int **list_a, int **list_b)
+{
+    *counters = pl->scratch;
+    *list_a = pl->scratch + 2;
+    *list_b = pl->scratch + 2 + pl->dev.n_out;
+    return IRC_OK;
+}
+
+int irc_site_knn_exact(irc_plan *pl, const float *F, int nC, int knn, float *vrKnn, float *rho,
+                       int32_t *miKnn, float *d2Knn, cudaStream_t s)
+{
+    if (knn > kCap / 2) { irc_host::set_error("irc_site_knn(EXACT): knn %d > %d", knn, kCap / 2); return IRC_E_INVAL; }
+    int *cnt, *la, *lb;
+    int rc = irc_plan_scratch(pl, &cnt, &la, &lb);
+    if (rc != IRC_OK) return rc;
+    cudaError_t e = cudaMemsetAsync(cnt, 0, 2 * sizeof(int), s);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(EXACT): memset");
+    const size_t smem = (size_t)kQB * kCap * 8 + (size_t)kQB * kThreads * 4;
+    e = cudaFuncSetAttribute(k_site_knn_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(EXACT): smem attribute");
+    const int tiles = pl->ntiles[irc::tile_slot(kQB)];
+    k_site_knn_exact<<<tiles, kThreads, smem, s>>>(pl->dev, F, nC, knn, vrKnn, rho, miKnn, d2Knn, cnt, la);
+    IRC_CHECK_LAUNCH("irc_site_knn(EXACT)");
+    // the overflow list is usually empty; size the grid for the worst case
+    k_exact_overflow<<<kQueueBlocks, 256, 0, s>>>(
+        pl->dev, F, nC, knn, cnt, la, vrKnn, rho, miKnn, d2Knn);
+    IRC_CHECK_LAUNCH("irc_site_knn(EXACT) overflow");
+    return IRC_OK;
+}
+
+int irc_site_delta_list(irc_plan *pl, const float *F, int nC, const float *R, int knn,
+                        const int32_t *miKnn, const float *d2Knn, float *delta, int32_t *nneigh,
+                        cudaStream_t s)
+{
+    int *cnt, *la, *lb;
+    int rc = irc_plan_scratch(pl, &cnt, &la, &lb);
+    if (rc != IRC_OK) return rc;
+    cudaError_t e = cudaMemsetAsync(cnt + 1, 0, sizeof(int), s);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_delta: memset");
+    const int n = pl->dev.n_out;
+    k_delta_list<<<(n + 255) / 256, 256, 0, s>>>(pl->dev, R, knn, miKnn, d2Knn, delta, nneigh, cnt + 1, lb);
+    IRC_CHECK_LAUNCH("irc_site_delta list");
+    k_delta_scan<<<kQueueBlocks, 256, 0, s>>>(pl->dev, F, R, nC, cnt + 1, lb,
+                                                                              delta, nneigh);
+    IRC_CHECK_LAUNCH("irc_site_delta scan");
+    return IRC_OK;
+}

@@ -1,0 +1,51 @@
+// irc_plan.cuh -- device-resident launch plan of one site (internal).
+#pragma once
+#include "irc_common.cuh"
+
+namespace irc {
+
+// Query-tile sizes for which a plan precomputes its tile tables.
+constexpr int kTileSizes[] = {8, 16, 32, 64, 128};
+constexpr int kNumTileSizes = 5;
+
+__host__ __device__ constexpr int tile_slot(int qb)
+{
+    return qb == 8 ? 0 : qb == 16 ? 1 : qb == 32 ? 2 : qb == 64 ? 3 : 4;
+}
+
+// Plain device pointers into one allocation owned by irc_plan.
+struct PlanDev {
+    const int32_t *q0, *nq, *roff, *rs, *rn;
+    const int32_t *tile_off[kNumTileSizes];   // [nChunks+1] prefix sums of ceil(nq/QB)
+    int nChunks, q_base, n_out, nF, nRuns;
+};
+
+// Map a flat tile id to (chunk, first query, query count) for tile size QB.
+template <int QB>
+__device__ __forceinline__ void tile_lookup(const PlanDev &p, int tile, int &chunk, int &qs, int &n)
+{
+    const int32_t *to = p.tile_off[tile_slot(QB)];
+    int lo = 0, hi = p.nChunks;            // find chunk with to[chunk] <= tile < to[chunk+1]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(to + mid) <= tile) lo = mid; else hi = mid;
+    }
+    chunk = lo;
+    const int qt = tile - __ldg(to + lo);
+    qs = __ldg(p.q0 + lo) + qt * QB;
+    n = min(QB, __ldg(p.nq + lo) - qt * QB);
+}
+
+}  // namespace irc
+
+struct irc_plan {
+    irc::PlanDev dev;
+    void *dmem;                            // single device allocation behind dev
+    int32_t *scratch;                      // inside dmem: 2 counters + 2 x n_out query lists
+    int ntiles[irc::kNumTileSizes];        // host copy of tile counts
+    int max_nq;                            // largest query chunk
+    long long pairs;                       // (query, candidate) pairs of the plan
+    int device;
+    // host copies (for the per-chunk drop-in emulation and validation)
+    int32_t *h_q0, *h_nq, *h_roff, *h_rs, *h_rn;
+};

@@ -1,0 +1,326 @@
+// irc_site.cu -- fused per-site path, REF mode, and plan management.
+//
+// The MATLAB host launches search_min_drift once per drift chunk, gathers the
+// [nT x nA] per-bin minima to the host and sorts every column there
+// (matlab/irc2.m:3764-3788); search_delta_drift is handled the same way with
+// a column `min` (:3829-3858).  Here one launch covers every chunk of a site:
+// a CTA owns a tile of up to QB queries of one chunk, evaluates every bin of
+// the chunk into shared memory, and performs the MATLAB sort/min on the
+// device with warp arg-min reductions over (value, bin) keys -- the stable
+// ascending order of MATLAB's sort.  Results equal the reference kernels +
+// MATLAB post-processing bit for bit.
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "irc_common.cuh"
+#include "irc_plan.cuh"
+#include "irc_scan.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kKnnQB = 16;     // queries per CTA, kNN kernel (bin table 16 x nT in smem)
+constexpr int kDeltaQB = 16;   // queries per CTA, delta kernel
+
+// kNN (search_min_drift + sort): bin table sV/sI [QB][nT] in dynamic smem.
+__global__ void __launch_bounds__(kThreads)
+k_site_knn_ref(irc::PlanDev p, const float *__restrict__ F, int nC, int nT, int knn,
+               float *__restrict__ vrKnn, float *__restrict__ rho, int *__restrict__ miKnn)
+{
+    constexpr int QB = kKnnQB;
+    __shared__ __align__(16) float sA[IRC_NC_MAX * QB];
+    extern __shared__ __align__(16) unsigned char dyn[];
+    float *sV = reinterpret_cast<float *>(dyn);            // [QB][nT]  sqrt(|bin min|)
+    int *sI = reinterpret_cast<int *>(sV + QB * nT);       // [QB][nT]  1-based index
+    int chunk, qs, n;
+    irc::tile_lookup<QB>(p, blockIdx.x, chunk, qs, n);
+    const int r0 = __ldg(p.roff + chunk), nBB = __ldg(p.roff + chunk + 1) - r0;
+    irc::stage_queries<QB>(F, nC, qs, n, sA);
+    __syncthreads();
+    const int nT0 = nT / nBB;
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        const int b = t % nBB;
+        const int ib0 = __ldg(p.rs + r0 + b), nb0 = __ldg(p.rn + r0 + b);
+        float mn[QB];
+        int mi[QB];
+#pragma unroll
+        for (int q = 0; q < QB; ++q) { mn[q] = IRC_SINGLE_INF_F; mi[q] = qs + min(q, n - 1); }
+        irc::scan_bin<QB, false>(F, nullptr, nC, ib0 + t / nBB, ib0 + nb0, nT0, sA, nullptr, mn, mi);
+#pragma unroll
+        for (int q = 0; q < QB; ++q) { sV[q * nT + t] = irc::ref_sqrt_abs(mn[q]); sI[q * nT + t] = mi[q] + 1; }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const float kTaken = -1.0f;
+    for (int q = warp; q < n; q += nw) {
+        float *v = sV + q * nT;
+        const int *ix = sI + q * nT;
+        const size_t o = (size_t)(qs + q - p.q_base);
+        float last = 0.0f;
+        for (int k = 0; k < knn; ++k) {
+            unsigned long long best = ~0ull;
+            for (int t = lane; t < nT; t += 32) {
+                const float x = v[t];
+                const unsigned long long key = (x == kTaken) ? ~0ull : irc::sort_key(x, t);
+                best = key < best ? key : best;
+            }
+            best = irc::warp_min_u64(best);
+            const int t = (int)(best & 0xffffffffu);
+            last = v[t];
+            __syncwarp();
+            if (lane == 0) {
+                miKnn[(size_t)k + (size_t)knn * o] = ix[t];
+                v[t] = kTaken;
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            vrKnn[o] = last;
+            if (rho) rho[o] = __fdiv_rn(1.0f, last);
+        }
+    }
+}
+
+// delta (search_delta_drift + min): thread-local arg-min over its bins, then a
+// block reduction of (value, bin) keys per query.
+__global__ void __launch_bounds__(kThreads)
+k_site_delta_ref(irc::PlanDev p, const float *__restrict__ F, const float *__restrict__ R, int nC,
+                 int nT, float *__restrict__ delta, int *__restrict__ nneigh)
+{
+    constexpr int QB = kDeltaQB;
+    __shared__ __align__(16) float sA[IRC_NC_MAX * QB];
+    __shared__ float sRA[QB];
+    __shared__ unsigned long long sKey[QB][kThreads / 32];
+    __shared__ int sIdx[QB][kThreads / 32];
+    int chunk, qs, n;
+    irc::tile_lookup<QB>(p, blockIdx.x, chunk, qs, n);
+    const int r0 = __ldg(p.roff + chunk), nBB = __ldg(p.roff + chunk + 1) - r0;
+    irc::stage_queries<QB>(F, nC, qs, n, sA);
+    if (threadIdx.x < QB) sRA[threadIdx.x] = __ldg(R + qs + min((int)threadIdx.x, n - 1));
+    __syncthreads();
+    const int nT0 = nT / nBB;
+    unsigned long long bk[QB];
+    int bi[QB];
+#pragma unroll
+    for (int q = 0; q < QB; ++q) { bk[q] = ~0ull; bi[q] = 0; }
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        const int b = t % nBB;
+        const int ib0 = __ldg(p.rs + r0 + b), nb0 = __ldg(p.rn + r0 + b);
+        float mn[QB];
+        int mi[QB];
+#pragma unroll
+        for (int q = 0; q < QB; ++q) { mn[q] = IRC_SINGLE_INF_F; mi[q] = qs + min(q, n - 1); }
+        irc::scan_bin<QB, true>(F, R, nC, ib0 + t / nBB, ib0 + nb0, nT0, sA, sRA, mn, mi);
+#pragma unroll
+        for (int q = 0; q < QB; ++q) {
+            const unsigned long long key = irc::sort_key(irc::ref_sqrt_abs(mn[q]), t);
+            if (key < bk[q]) { bk[q] = key; bi[q] = mi[q]; }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+        unsigned long long k = bk[q];
+        int idx = bi[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+            if (ok < k) { k = ok; idx = oi; }
+        }
+        if (lane == 0) { sKey[q][warp] = k; sIdx[q][warp] = idx; }
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        const int q = threadIdx.x;
+        unsigned long long k = sKey[q][0];
+        int idx = sIdx[q][0];
+        for (int w = 1; w < kThreads / 32; ++w)
+            if (sKey[q][w] < k) { k = sKey[q][w]; idx = sIdx[q][w]; }
+        const float v = __uint_as_float((unsigned)(k >> 32));
+        const size_t o = (size_t)(qs + q - p.q_base);
+        delta[o] = __fmul_rn(v, sRA[q]);
+        nneigh[o] = idx + 1;
+    }
+}
+
+inline int tiles_for(const irc_plan *pl, int qb) { return pl->ntiles[irc::tile_slot(qb)]; }
+
+}  // namespace
+
+int irc_exact_chunk_fill(float *, int32_t *, const float *, const int32_t *, const int32_t *, int,
+                         int, int, int, int, int, cudaStream_t)
+{
+    irc_host::set_error("irc_search_min_drift: IRC_MODE_EXACT is served by irc_site_knn");
+    return IRC_E_UNSUPPORTED;
+}
+
+// Exact / tensor-core site kernels (irc_exact.cu, irc_tc.cu).
+int irc_site_knn_exact(irc_plan *plan, const float *F, int nC, int knn, float *vrKnn, float *rho,
+                       int32_t *miKnn, float *d2Knn, cudaStream_t s);
+int irc_site_knn_tc(irc_plan *plan, const float *F, int nC, int knn, int mode, float *vrKnn,
+                    float *rho, int32_t *miKnn, float *d2Knn, cudaStream_t s);
+int irc_site_delta_list(irc_plan *plan, const float *F, int nC, const float *R, int knn,
+                        const int32_t *miKnn, const float *d2Knn, float *delta, int32_t *nneigh,
+                        cudaStream_t s);
+
+extern "C" {
+
+int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                    const int32_t *rs, const int32_t *rn, int nChunks, int q_base, int n_out, int nF)
+{
+    if (!out || !q0 || !nq || !roff || !rs || !rn || nChunks <= 0 || n_out <= 0 || nF <= 0) {
+        irc_host::set_error("irc_plan_create: null pointer or empty plan");
+        return IRC_E_INVAL;
+    }
+    *out = nullptr;
+    const int nRuns = roff[nChunks];
+    if (roff[0] != 0 || nRuns <= 0) { irc_host::set_error("irc_plan_create: bad roff"); return IRC_E_INVAL; }
+    long long pairs = 0;
+    int max_nq = 0;
+    for (int i = 0; i < nChunks; ++i) {
+        if (nq[i] <= 0 || q0[i] < 0 || q0[i] + nq[i] > nF || q0[i] < q_base || q0[i] + nq[i] > q_base + n_out ||
+            roff[i + 1] <= roff[i]) {
+            irc_host::set_error("irc_plan_create: chunk %d out of range", i);
+            return IRC_E_INVAL;
+        }
+        long long cand = 0;
+        for (int r = roff[i]; r < roff[i + 1]; ++r) {
+            if (rs[r] < 0 || rn[r] <= 0 || (long long)rs[r] + rn[r] > nF) {
+                irc_host::set_error("irc_plan_create: run %d out of range", r);
+                return IRC_E_INVAL;
+            }
+            cand += rn[r];
+        }
+        pairs += cand * nq[i];
+        max_nq = nq[i] > max_nq ? nq[i] : max_nq;
+    }
+    irc_plan *pl = (irc_plan *)calloc(1, sizeof(irc_plan));
+    if (!pl) return IRC_E_NOMEM;
+    // host copies
+    const size_t nCh = (size_t)nChunks;
+    pl->h_q0 = (int32_t *)malloc(4 * nCh);
+    pl->h_nq = (int32_t *)malloc(4 * nCh);
+    pl->h_roff = (int32_t *)malloc(4 * (nCh + 1));
+    pl->h_rs = (int32_t *)malloc(4 * (size_t)nRuns);
+    pl->h_rn = (int32_t *)malloc(4 * (size_t)nRuns);
+    memcpy(pl->h_q0, q0, 4 * nCh);
+    memcpy(pl->h_nq, nq, 4 * nCh);
+    memcpy(pl->h_roff, roff, 4 * (nCh + 1));
+    memcpy(pl->h_rs, rs, 4 * (size_t)nRuns);
+    memcpy(pl->h_rn, rn, 4 * (size_t)nRuns);
+    // device image: q0 | nq | roff | rs | rn | tile_off x 5
+    std::vector<int32_t> img;
+    img.reserve(4 * nCh + 2 * nRuns + irc::kNumTileSizes * (nCh + 1) + 8);
+    size_t off_q0 = img.size(); img.insert(img.end(), q0, q0 + nCh);
+    size_t off_nq = img.size(); img.insert(img.end(), nq, nq + nCh);
+    size_t off_roff = img.size(); img.insert(img.end(), roff, roff + nCh + 1);
+    size_t off_rs = img.size(); img.insert(img.end(), rs, rs + nRuns);
+    size_t off_rn = img.size(); img.insert(img.end(), rn, rn + nRuns);
+    size_t off_tile[irc::kNumTileSizes];
+    for (int k = 0; k < irc::kNumTileSizes; ++k) {
+        const int qb = irc::kTileSizes[k];
+        off_tile[k] = img.size();
+        int acc = 0;
+        img.push_back(0);
+        for (int i = 0; i < nChunks; ++i) { acc += (nq[i] + qb - 1) / qb; img.push_back(acc); }
+        pl->ntiles[k] = acc;
+    }
+    cudaGetDevice(&pl->device);
+    const size_t scratch_ints = 2 + 2 * (size_t)n_out;
+    cudaError_t e = cudaMalloc(&pl->dmem, (img.size() + scratch_ints) * sizeof(int32_t));
+    if (e != cudaSuccess) {
+        free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn); free(pl);
+        irc_host::cuda_status(e, "irc_plan_create: cudaMalloc");
+        return IRC_E_NOMEM;
+    }
+    e = cudaMemcpy(pl->dmem, img.data(), img.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cudaFree(pl->dmem); free(pl); return irc_host::cuda_status(e, "irc_plan_create: upload"); }
+    const int32_t *base = (const int32_t *)pl->dmem;
+    pl->dev.q0 = base + off_q0;
+    pl->dev.nq = base + off_nq;
+    pl->dev.roff = base + off_roff;
+    pl->dev.rs = base + off_rs;
+    pl->dev.rn = base + off_rn;
+    for (int k = 0; k < irc::kNumTileSizes; ++k) pl->dev.tile_off[k] = base + off_tile[k];
+    pl->scratch = (int32_t *)pl->dmem + img.size();
+    pl->dev.nChunks = nChunks;
+    pl->dev.q_base = q_base;
+    pl->dev.n_out = n_out;
+    pl->dev.nF = nF;
+    pl->dev.nRuns = nRuns;
+    pl->max_nq = max_nq;
+    pl->pairs = pairs;
+    *out = pl;
+    return IRC_OK;
+}
+
+int irc_plan_destroy(irc_plan *pl)
+{
+    if (!pl) return IRC_OK;
+    cudaError_t e = cudaFree(pl->dmem);
+    free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn);
+    free(pl);
+    return e == cudaSuccess ? IRC_OK : irc_host::cuda_status(e, "irc_plan_destroy");
+}
+
+int irc_site_knn(irc_plan *pl, const float *F, int nC, int knn, int nThreads, int mode,
+                 float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, void *stream)
+{
+    if (!pl || !F || !vrKnn || !miKnn) { irc_host::set_error("irc_site_knn: null pointer"); return IRC_E_INVAL; }
+    if (nC > IRC_NC_MAX) { irc_host::set_error("irc_site_knn: nC=%d > %d", nC, IRC_NC_MAX); return IRC_E_NC; }
+    if (nC <= 0 || knn <= 0) { irc_host::set_error("irc_site_knn: bad nC/knn"); return IRC_E_INVAL; }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (mode == IRC_MODE_REF) {
+        if (nThreads <= 0 || nThreads > 1024 || knn > nThreads) {
+            irc_host::set_error("irc_site_knn: bad nThreads=%d / knn=%d", nThreads, knn);
+            return IRC_E_INVAL;
+        }
+        for (int i = 0; i < pl->dev.nChunks; ++i)
+            if (pl->h_roff[i + 1] - pl->h_roff[i] > nThreads) {
+                irc_host::set_error("irc_site_knn: chunk %d has more runs than bins", i);
+                return IRC_E_INVAL;
+            }
+        const size_t smem = (size_t)kKnnQB * nThreads * 8;
+        cudaError_t e = cudaFuncSetAttribute(k_site_knn_ref, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn: smem attribute");
+        k_site_knn_ref<<<tiles_for(pl, kKnnQB), kThreads, smem, s>>>(pl->dev, F, nC, nThreads, knn, vrKnn, rho, miKnn);
+        IRC_CHECK_LAUNCH("irc_site_knn(REF)");
+        return IRC_OK;
+    }
+    if (mode == IRC_MODE_EXACT) return irc_site_knn_exact(pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
+    if (mode == IRC_MODE_BF16 || mode == IRC_MODE_FP8)
+        return irc_site_knn_tc(pl, F, nC, knn, mode, vrKnn, rho, miKnn, d2Knn, s);
+    irc_host::set_error("irc_site_knn: unknown mode %d", mode);
+    return IRC_E_INVAL;
+}
+
+int irc_site_delta(irc_plan *pl, const float *F, int nC, const float *R, int nThreads, int mode,
+                   int knn, const int32_t *miKnn, const float *d2Knn, float *delta, int32_t *nneigh,
+                   void *stream)
+{
+    if (!pl || !F || !R || !delta || !nneigh) { irc_host::set_error("irc_site_delta: null pointer"); return IRC_E_INVAL; }
+    if (nC > IRC_NC_MAX) { irc_host::set_error("irc_site_delta: nC=%d > %d", nC, IRC_NC_MAX); return IRC_E_NC; }
+    if (nC <= 0) { irc_host::set_error("irc_site_delta: bad nC"); return IRC_E_INVAL; }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (mode == IRC_MODE_REF) {
+        if (nThreads <= 0 || nThreads > 1024) { irc_host::set_error("irc_site_delta: bad nThreads"); return IRC_E_INVAL; }
+        for (int i = 0; i < pl->dev.nChunks; ++i)
+            if (pl->h_roff[i + 1] - pl->h_roff[i] > nThreads) {
+                irc_host::set_error("irc_site_delta: chunk %d has more runs than bins", i);
+                return IRC_E_INVAL;
+            }
+        k_site_delta_ref<<<tiles_for(pl, kDeltaQB), kThreads, 0, s>>>(pl->dev, F, R, nC, nThreads, delta, nneigh);
+        IRC_CHECK_LAUNCH("irc_site_delta(REF)");
+        return IRC_OK;
+    }
+    if (mode == IRC_MODE_EXACT || mode == IRC_MODE_BF16 || mode == IRC_MODE_FP8) {
+        if (!miKnn || !d2Knn || knn <= 0) { irc_host::set_error("irc_site_delta: kNN list required"); return IRC_E_INVAL; }
+        return irc_site_delta_list(pl, F, nC, R, knn, miKnn, d2Knn, delta, nneigh, s);
+    }
+    irc_host::set_error("irc_site_delta: unknown mode %d", mode);
+    return IRC_E_INVAL;
+}
+
+}  // extern "C"

@@ -1,0 +1,225 @@
+"""Drift linkage, paging and per-chunk launch plans (host side, numpy).
+
+Mirrors the irc2 host logic that sits around the hot-path kernels:
+
+* ``calc_drift``        calc_drift_        matlab/irc2.m:6373-6451
+* ``dist_mask_ml``      dist_mask_ml_      matlab/irc2.m:6455-6465
+* ``mi2ml_drift``       mi2ml_drift_       matlab/irc2.m:6509-6516
+* ``quantile_vr`` / ``subsample_vr``       matlab/irc2.m:6481-6490, :1557-1573
+* ``plan_sort_page``    plan_sort_page_    matlab/irc2.m:3914-3946
+* ``build_plan``        the per-chunk run selection inside search_knn_drift_ /
+                        search_delta_drift_, matlab/irc2.m:3752-3760,
+                        :3764-3773 and :3808-3812, :3829-3837
+
+Indices are 0-based here; chunk ids are 0-based (MATLAB's discretize gives
+1-based ids, the shift is applied at the MEX/MATLAB boundary only).
+
+A *plan* is the compact description of every kernel launch the MATLAB loop
+would make for one site: for query chunk i, queries ``[q0[i], q0[i]+nq[i])``
+(positions in the site feature matrix) and candidate runs
+``rs[roff[i]:roff[i+1]]`` / ``rn[...]`` (0-based run start and length; the
+IBB/NBB arguments of search_min_drift).  Outputs are indexed by
+``q - q_base`` with ``n_out`` rows.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def matlab_round(x):
+    """MATLAB round: halves away from zero."""
+    x = np.asarray(x, dtype=np.float64)
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def subsample_vr(vi, n_max):
+    """subsample_vr_ (matlab/irc2.m:1557-1573)."""
+    vi = np.asarray(vi)
+    if vi.size > n_max:
+        n_skip = vi.size // n_max
+        if n_skip > 1:
+            vi = vi[::n_skip]
+        if vi.size > n_max:
+            n_remove = vi.size - n_max
+            rm = matlab_round(np.linspace(1, vi.size, n_remove)).astype(np.int64)
+            rm = np.clip(rm, 1, vi.size) - 1
+            keep = np.ones(vi.size, bool)
+            keep[rm] = False
+            vi = vi[keep]
+    return vi
+
+
+def quantile_vr(vr, vr_q, max_sample=100000):
+    """quantile_vr_ (matlab/irc2.m:6481-6490)."""
+    vr = subsample_vr(np.asarray(vr), max_sample)
+    n = vr.size
+    idx = np.maximum(np.minimum(matlab_round(n * np.asarray(vr_q, np.float64)), n), 1).astype(np.int64)
+    return np.sort(vr, kind="stable")[idx - 1]
+
+
+def histcounts2(x, y, xedges, yedges):
+    """MATLAB histcounts2: bins [e_i, e_{i+1}), the last bin closed."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    xe = np.asarray(xedges, np.float64)
+    ye = np.asarray(yedges, np.float64)
+    nx, ny = xe.size - 1, ye.size - 1
+    ix = np.searchsorted(xe, x, side="right") - 1
+    iy = np.searchsorted(ye, y, side="right") - 1
+    ix[x == xe[-1]] = nx - 1
+    iy[y == ye[-1]] = ny - 1
+    ok = (ix >= 0) & (ix < nx) & (iy >= 0) & (iy < ny) & (x >= xe[0]) & (y >= ye[0])
+    out = np.zeros((nx, ny), np.float64)
+    np.add.at(out, (ix[ok], iy[ok]), 1)
+    return out
+
+
+def mi2ml_drift(mi_member):
+    """mi2ml_drift_: column j of the result marks the chunks listed in column j."""
+    mi_member = np.asarray(mi_member)
+    n_members, n_drift = mi_member.shape
+    ml = np.zeros((n_drift, n_drift), bool)
+    ml[mi_member.ravel(order="F"), np.repeat(np.arange(n_drift), n_members)] = True
+    return ml
+
+
+def dist_mask_ml(mrF, ml_mask, nneigh):
+    """dist_mask_ml_: per column, the nneigh nearest masked columns of mrF
+    (Euclidean, stable ascending sort).  mrF: [nFeat, nDrift]."""
+    mrF = np.asarray(mrF, np.float64)
+    n = mrF.shape[1]
+    ml = np.zeros((n, n), bool)
+    for j in range(n):
+        rows = np.flatnonzero(ml_mask[:, j])
+        d = np.sqrt(((mrF[:, [j]] - mrF[:, rows]) ** 2).sum(0))
+        srt = np.argsort(d, kind="stable")
+        ml[rows[srt[:nneigh]], j] = True
+    return ml
+
+
+def drift_mask(n_drift, quarter):
+    """The |i-j| <= quarter band with the edge blocks calc_drift_ adds
+    (matlab/irc2.m:6425-6431)."""
+    i = np.arange(n_drift)
+    m = np.abs(i[None, :] - i[:, None]) <= quarter
+    m[: quarter * 2 + 1, :quarter] = True
+    m[-(quarter * 2 + 1):, -quarter:] = True
+    return m
+
+
+def calc_drift(vrAmp_spk, vrPos_spk, n_sites, nTime_drift, nTime_batch, nTime_max_drift=256,
+               nQuantile_drift=10):
+    """calc_drift_ (matlab/irc2.m:6373-6451) without its parfor/plot branches.
+
+    Returns (viLim_drift, mlDrift): 0-based chunk limits [nTime_drift+1]
+    (chunk i = spikes viLim[i]..viLim[i+1]-1) and the linkage matrix.
+    """
+    n_spk = len(vrAmp_spk)
+    if not nTime_batch or not nTime_drift or nTime_batch >= nTime_drift:
+        return np.array([0, n_spk], np.int64), np.ones((1, 1), bool)
+    lim = np.concatenate([[0], np.ceil(np.arange(1, nTime_drift + 1) / nTime_drift * n_spk)]).astype(np.int64)
+    amp = np.asarray(vrAmp_spk, np.float32)
+    pos = np.asarray(vrPos_spk, np.float32)
+    amp_q = quantile_vr(amp, np.arange(nQuantile_drift + 1) / nQuantile_drift)
+    pos_q = quantile_vr(pos, np.arange(n_sites + 1) / n_sites)
+    counts = np.zeros((nQuantile_drift * n_sites, nTime_drift), np.float32)
+    for i in range(nTime_drift):
+        h = histcounts2(amp[lim[i]:lim[i + 1]], pos[lim[i]:lim[i + 1]], amp_q, pos_q)
+        counts[:, i] = h.ravel(order="F")
+    if nTime_drift > nTime_max_drift:
+        quarter = nTime_max_drift // 4
+        ml = dist_mask_ml(counts, drift_mask(nTime_drift, quarter), nTime_batch)
+    else:
+        d = np.sqrt(((counts[:, :, None] - counts[:, None, :]).astype(np.float64) ** 2).sum(0))
+        mi = np.argsort(d, axis=0, kind="stable")[:nTime_batch, :]
+        ml = mi2ml_drift(mi)
+    return lim, ml
+
+
+def plan_sort_page(nTime_drift, viLim_drift, nTime_max_drift=256):
+    """plan_sort_page_ (matlab/irc2.m:3914-3946), 0-based.
+
+    Returns a list of pages: dict(drift_out=(a, b), drift_in=(a, b),
+    spk_out=(s0, s1), spk_in=(s0, s1)) with inclusive chunk ranges and
+    half-open spike ranges."""
+    n = nTime_drift
+    width = nTime_max_drift
+    quarter, half = width // 4, width // 2
+    n_pages = n // half
+    lim = np.asarray(viLim_drift)
+    if n_pages == 0:
+        return [dict(drift_out=(0, n - 1), drift_in=(0, n - 1),
+                     spk_out=(int(lim[0]), int(lim[-1])), spk_in=(int(lim[0]), int(lim[-1])))]
+    pages, ib_prev = [], 0
+    for p in range(1, n_pages + 1):
+        iB = min((p - 1) * half + width, n)
+        iA = max(1, iB - width + 1)
+        ia = 1 if p == 1 else min(iA + quarter, n)
+        ia = max(ib_prev + 1, ia)
+        ib = n if p == n_pages else max(iB - quarter, 1)
+        ib_prev = ib
+        pages.append(dict(drift_out=(iA - 1, iB - 1), drift_in=(ia - 1, ib - 1),
+                          spk_out=(int(lim[iA - 1]), int(lim[iB])),
+                          spk_in=(int(lim[ia - 1]), int(lim[ib]))))
+    return pages
+
+
+def build_plan(viDrift_out, vl_in, mlDrift):
+    """Per-chunk launch plan of search_knn_drift_ (matlab/irc2.m:3752-3787).
+
+    viDrift_out: chunk id of every column of the site feature matrix (primary
+    spikes sorted by time, then optional secondary-site copies).  vl_in:
+    boolean mask of the query columns (a contiguous range).  mlDrift: [nDrift
+    x nDrift] boolean; column a lists the chunks linked to chunk a."""
+    vd = np.asarray(viDrift_out).astype(np.int64).ravel()
+    vl = np.asarray(vl_in).astype(bool).ravel()
+    ml = np.asarray(mlDrift).astype(bool)
+    if not vl.any():
+        raise ValueError("build_plan: no query spikes")
+    in_idx = np.flatnonzero(vl)
+    in_offset = int(in_idx[0])
+    if in_idx[-1] - in_offset + 1 != in_idx.size:
+        raise ValueError("build_plan: query columns must be contiguous")
+    vd_in = vd[vl]
+    change = np.flatnonzero(np.diff(vd)) + 1
+    viiBB = np.concatenate([[0], change, [vd.size]]).astype(np.int64)
+    viBB = vd[viiBB[:-1]]
+    vnBB = np.diff(viiBB)
+    q0, nq, roff, rs, rn = [], [], [0], [], []
+    for a in range(int(vd_in.min()), int(vd_in.max()) + 1):
+        vii = np.flatnonzero(vd_in == a)
+        if vii.size == 0:
+            continue
+        lo, hi = int(vii[0]) + in_offset, int(vii[-1]) + in_offset
+        if hi - lo + 1 != vii.size:
+            raise ValueError("build_plan: chunk %d queries are not contiguous" % a)
+        linked = np.flatnonzero(ml[:, a])
+        runs = np.flatnonzero(np.isin(viBB, linked))
+        q0.append(lo)
+        nq.append(hi - lo + 1)
+        rs.extend(viiBB[runs].tolist())
+        rn.extend(vnBB[runs].tolist())
+        roff.append(len(rs))
+    i32 = lambda v: np.asarray(v, np.int32)
+    return dict(q0=i32(q0), nq=i32(nq), roff=i32(roff), rs=i32(rs), rn=i32(rn),
+                q_base=in_offset, n_out=int(vl.sum()), n_f=int(vd.size))
+
+
+def plan_pairs(plan):
+    """Number of (query, candidate) pairs the plan evaluates."""
+    roff, rn, nq = plan["roff"], plan["rn"].astype(np.int64), plan["nq"].astype(np.int64)
+    per_chunk = np.array([rn[roff[i]:roff[i + 1]].sum() for i in range(len(nq))], np.int64)
+    return int((per_chunk * nq).sum())
+
+
+def plan_chunk(plan, i):
+    """(IBB, NBB, vnConst-without-nC/nF) of query chunk i."""
+    r0, r1 = int(plan["roff"][i]), int(plan["roff"][i + 1])
+    return plan["rs"][r0:r1], plan["rn"][r0:r1], int(plan["q0"][i]), int(plan["nq"][i])
+
+
+def chunk_limits(n_spk, n_chunks):
+    """Equal-count chunk limits, 0-based: ceil((1:n)/n * N) (matlab/irc2.m:6395)."""
+    return np.concatenate([[0], [math.ceil(i / n_chunks * n_spk) for i in range(1, n_chunks + 1)]]).astype(np.int64)

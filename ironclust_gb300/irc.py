@@ -1,0 +1,338 @@
+"""Host-side mirror of IronClust's MATLAB hot-path wrappers over the C ABI.
+
+The reference host is MATLAB; this module restates its wrappers in Python
+so they can drive the sm_103a library (libircgb300.so) the way the MATLAB
+code drives the reference kernels, and so the parity tests read like the
+reference's call sites.  PyTorch only provides device memory and streams.
+
+Feature matrices are torch float32 CUDA tensors of shape [n, nC] (C order),
+which is byte-identical to MATLAB's column-major [nC x n].  Kernel outputs
+MATLAB sees as [nT x nA] are returned as [nA, nT] tensors (same bytes).
+
+Reference call sites mirrored here:
+  search_knn_drift_    matlab/irc2.m:3731-3789   -> search_knn_drift
+  search_delta_drift_  matlab/irc2.m:3794-3865   -> search_delta_drift_host
+  rho_paged_site_      matlab/irc2.m:3635-3680   -> rho_site
+  delta_paged_site_    matlab/irc2.m:3684-3726   -> delta_site
+  sort_ normalisation  matlab/irc2.m:3263-3271   -> normalize_rho
+  cuda_knn_            matlab/irc.m:24365-24401  -> cuda_knn
+  cuda_delta_knn_      matlab/irc.m:24519-24553  -> cuda_delta_knn_host
+  cuda_rho_drift_      matlab/irc.m:24612-24637  -> cuda_rho_drift
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib
+from .drift import build_plan
+
+SINGLE_INF = 3.402e38                       # MATLAB double literal
+SQRT_SINGLE_INF_F = np.float32(np.sqrt(SINGLE_INF))   # single(sqrt(SINGLE_INF)), matlab/irc2.m:3725
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _i32host(v):
+    return np.ascontiguousarray(v, dtype=np.int32)
+
+
+def _dev_f32(x, device="cuda"):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=torch.float32).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(device)
+
+
+def _dev_i32(x, device="cuda"):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=torch.int32).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.int32)).to(device)
+
+
+def _mode(mode):
+    return _lib.MODES[mode] if isinstance(mode, str) else int(mode)
+
+
+# ---------------------------------------------------------------------------
+# drop-in kernels (one call == one MATLAB feval)
+# ---------------------------------------------------------------------------
+
+def search_min_drift(F, IBB, NBB, vnConst, nThreads=1024, mode="ref", knn=30):
+    """feval(search_min_drift, D, I, F, IBB, NBB, vnConst); returns (D, I) as [nA, nThreads]."""
+    vn = _i32host(vnConst)
+    nA = int(vn[4])
+    D = torch.empty((nA, nThreads), dtype=torch.float32, device=F.device)
+    I = torch.empty((nA, nThreads), dtype=torch.int32, device=F.device)
+    check(lib().irc_search_min_drift(_p(D), _p(I), _p(F), _p(IBB), _p(NBB),
+                                     vn.ctypes.data_as(C.c_void_p), nThreads, _mode(mode), knn,
+                                     _stream()), "irc_search_min_drift")
+    return D, I
+
+
+def search_delta_drift(F, R, IBB, NBB, vnConst, nThreads=512):
+    vn = _i32host(vnConst)
+    nA = int(vn[4])
+    D = torch.empty((nA, nThreads), dtype=torch.float32, device=F.device)
+    I = torch.empty((nA, nThreads), dtype=torch.int32, device=F.device)
+    check(lib().irc_search_delta_drift(_p(D), _p(I), _p(F), _p(R), _p(IBB), _p(NBB),
+                                       vn.ctypes.data_as(C.c_void_p), nThreads, _stream()),
+          "irc_search_delta_drift")
+    return D, I
+
+
+def cuda_knn_index(B, A, knn, nThreads=512):
+    """feval(cuda_knn_index, K, I, B, A, vnConst); returns K [nA], I [nA, knn]."""
+    nB, nA, nC = B.shape[0], A.shape[0], A.shape[1]
+    vn = _i32host([nB, nA, nC, knn])
+    K = torch.empty(nA, dtype=torch.float32, device=A.device)
+    I = torch.empty((nA, knn), dtype=torch.int32, device=A.device)
+    check(lib().irc_cuda_knn_index(_p(K), _p(I), _p(B), _p(A), vn.ctypes.data_as(C.c_void_p),
+                                   nThreads, _stream()), "irc_cuda_knn_index")
+    return K, I
+
+
+def cuda_delta_knn(B, A, R_B, R_A, nThreads=128):
+    """feval(cuda_delta_knn, D, N, B, A, R_B, R_A, vnConst); returns D [nA], N [nA] (uint32 bits in int32)."""
+    nB, nA, nC = B.shape[0], A.shape[0], A.shape[1]
+    vn = _i32host([nB, nA, nC])
+    D = torch.empty(nA, dtype=torch.float32, device=A.device)
+    N = torch.empty(nA, dtype=torch.int32, device=A.device)
+    check(lib().irc_cuda_delta_knn(_p(D), _p(N), _p(B), _p(A), _p(R_B), _p(R_A),
+                                   vn.ctypes.data_as(C.c_void_p), nThreads, _stream()),
+          "irc_cuda_delta_knn")
+    return D, N
+
+
+def rho_drift(miSite12_colmajor, mrFet1, mrFet2, n1, dc2):
+    """feval(jrc3_cuda_rho_drift, vrRho1, miSite12, mrFet1, mrFet2, vnConst, dc2).
+    miSite12_colmajor: int32 device tensor of 2*n12 entries (MATLAB [n12 x 2])."""
+    n12, nC = mrFet1.shape
+    vn = _i32host([n1, n12, nC])
+    rho = torch.empty(n1, dtype=torch.float32, device=mrFet1.device)
+    check(lib().irc_rho_drift(_p(rho), _p(miSite12_colmajor), _p(mrFet1), _p(mrFet2),
+                              vn.ctypes.data_as(C.c_void_p), C.c_float(dc2), _stream()),
+          "irc_rho_drift")
+    return rho
+
+
+# ---------------------------------------------------------------------------
+# MATLAB post-processing on the device
+# ---------------------------------------------------------------------------
+
+def matlab_sort_knn(D, I, knn):
+    """[vs, ord] = sort(D) (stable, NaN last); vrKnn = vs(knn,:); miKnn = I(ord(1:knn,:))."""
+    key = torch.where(torch.isnan(D), torch.full_like(D, float("inf")), D)
+    nanrank = torch.isnan(D).to(torch.int8)
+    # stable sort by value, then a stable sort by the NaN flag keeps NaN last
+    v, order = torch.sort(key, dim=1, stable=True)
+    order = torch.gather(order, 1, torch.argsort(torch.gather(nanrank, 1, order), dim=1, stable=True))
+    vs = torch.gather(D, 1, order)
+    return vs[:, knn - 1].contiguous(), torch.gather(I, 1, order[:, :knn]).contiguous()
+
+
+def matlab_min(D, I):
+    """[vrMin, viMin] = min(D) over columns (first index, NaN skipped)."""
+    key = torch.where(torch.isnan(D), torch.full_like(D, float("inf")), D)
+    m = key.min(dim=1, keepdim=True).values
+    first = (key == m).to(torch.int8).argmax(dim=1, keepdim=True)
+    return torch.gather(D, 1, first).squeeze(1), torch.gather(I, 1, first).squeeze(1)
+
+
+# ---------------------------------------------------------------------------
+# per-chunk MATLAB loops (the unchanged host driving the drop-in kernels)
+# ---------------------------------------------------------------------------
+
+def search_knn_drift(plan, F, knn=30, nThreads=1024, mode="ref"):
+    """search_knn_drift_ (matlab/irc2.m:3731-3789): one drop-in launch per
+    drift chunk plus the MATLAB column sort.  Returns vrKnn [n_out], miKnn
+    [n_out, knn] (1-based into F)."""
+    n_out = plan["n_out"]
+    vrKnn = torch.zeros(n_out, dtype=torch.float32, device=F.device)
+    miKnn = torch.zeros((n_out, knn), dtype=torch.int32, device=F.device)
+    nC, nF = F.shape[1], F.shape[0]
+    for i in range(len(plan["q0"])):
+        r0, r1 = int(plan["roff"][i]), int(plan["roff"][i + 1])
+        IBB = _dev_i32(plan["rs"][r0:r1], F.device)
+        NBB = _dev_i32(plan["rn"][r0:r1], F.device)
+        q0, nq = int(plan["q0"][i]), int(plan["nq"][i])
+        D, I = search_min_drift(F, IBB, NBB, [nC, nF, r1 - r0, q0, nq], nThreads, mode, knn)
+        v, m = matlab_sort_knn(D, I, knn)
+        o = q0 - plan["q_base"]
+        vrKnn[o:o + nq] = v
+        miKnn[o:o + nq] = m
+    return vrKnn, miKnn
+
+
+def search_delta_drift_host(plan, F, R, nThreads=512):
+    """search_delta_drift_ (matlab/irc2.m:3794-3865): per-chunk launch + column min."""
+    n_out = plan["n_out"]
+    vrDelta = torch.zeros(n_out, dtype=torch.float32, device=F.device)
+    viNneigh = torch.zeros(n_out, dtype=torch.int32, device=F.device)
+    nC, nF = F.shape[1], F.shape[0]
+    for i in range(len(plan["q0"])):
+        r0, r1 = int(plan["roff"][i]), int(plan["roff"][i + 1])
+        IBB = _dev_i32(plan["rs"][r0:r1], F.device)
+        NBB = _dev_i32(plan["rn"][r0:r1], F.device)
+        q0, nq = int(plan["q0"][i]), int(plan["nq"][i])
+        D, I = search_delta_drift(F, R, IBB, NBB, [nC, nF, r1 - r0, q0, nq], nThreads)
+        v, m = matlab_min(D, I)
+        o = q0 - plan["q_base"]
+        vrDelta[o:o + nq] = v
+        viNneigh[o:o + nq] = m
+    return vrDelta, viNneigh
+
+
+# ---------------------------------------------------------------------------
+# fused per-site path
+# ---------------------------------------------------------------------------
+
+class Plan:
+    """Device-resident launch plan of one site (irc_plan_create)."""
+
+    def __init__(self, plan):
+        self.d = plan
+        self.h = C.c_void_p()
+        arrs = [_i32host(plan[k]) for k in ("q0", "nq", "roff", "rs", "rn")]
+        self._keep = arrs
+        check(lib().irc_plan_create(C.byref(self.h), *[a.ctypes.data_as(C.c_void_p) for a in arrs],
+                                    len(arrs[0]), int(plan["q_base"]), int(plan["n_out"]),
+                                    int(plan["n_f"])), "irc_plan_create")
+
+    @classmethod
+    def from_drift(cls, viDrift_out, vl_in, mlDrift):
+        return cls(build_plan(viDrift_out, vl_in, mlDrift))
+
+    @property
+    def n_out(self):
+        return int(self.d["n_out"])
+
+    def close(self):
+        if self.h:
+            lib().irc_plan_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def site_knn(plan, F, knn=30, mode="ref", nThreads=1024, want_d2=None):
+    """irc_site_knn: kNN + rho of every query of the plan.
+    Returns dict(vrKnn, rho, miKnn [n_out, knn] 1-based, d2Knn or None)."""
+    n = plan.n_out
+    dev = F.device
+    vrKnn = torch.empty(n, dtype=torch.float32, device=dev)
+    rho = torch.empty(n, dtype=torch.float32, device=dev)
+    miKnn = torch.empty((n, knn), dtype=torch.int32, device=dev)
+    m = _mode(mode)
+    if want_d2 is None:
+        want_d2 = m != _lib.MODE_REF
+    d2 = torch.empty((n, knn), dtype=torch.float32, device=dev) if want_d2 else None
+    check(lib().irc_site_knn(plan.h, _p(F), F.shape[1], knn, nThreads, m, _p(vrKnn), _p(rho),
+                             _p(miKnn), _p(d2), _stream()), "irc_site_knn")
+    return dict(vrKnn=vrKnn, rho=rho, miKnn=miKnn, d2Knn=d2)
+
+
+def site_delta(plan, F, R, mode="ref", nThreads=512, knn=30, miKnn=None, d2Knn=None):
+    """irc_site_delta: delta (= nearest higher-rho distance .* rho) and nneigh (1-based)."""
+    n = plan.n_out
+    delta = torch.empty(n, dtype=torch.float32, device=F.device)
+    nneigh = torch.empty(n, dtype=torch.int32, device=F.device)
+    check(lib().irc_site_delta(plan.h, _p(F), F.shape[1], _p(R), nThreads, _mode(mode), knn,
+                               _p(miKnn), _p(d2Knn), _p(delta), _p(nneigh), _stream()),
+          "irc_site_delta")
+    return delta, nneigh
+
+
+def knn_rho_delta_site(plan, F, knn=30, mode="ref", nThreads_rho=1024, nThreads_delta=512):
+    """One single-page site end to end: kNN, rho = 1/d_knn, delta, nneigh.
+    Requires every column of F to be a query (the plan covers all of F)."""
+    if plan.n_out != F.shape[0] or int(plan.d["q_base"]) != 0:
+        raise ValueError("knn_rho_delta_site: the plan must cover every column of F")
+    k = site_knn(plan, F, knn, mode, nThreads_rho)
+    delta, nneigh = site_delta(plan, F, k["rho"], mode, nThreads_delta, knn, k["miKnn"], k["d2Knn"])
+    k.update(delta=delta, nneigh=nneigh)
+    return k
+
+
+# ---------------------------------------------------------------------------
+# rho_paged_site_ / delta_paged_site_ / sort_ post-processing (host logic)
+# ---------------------------------------------------------------------------
+
+def rho_post(vrKnn, miKnn, viSpk_out, knn):
+    """rho = 1 ./ vrKnn; miKnn -> global int64 ids; pad rows to knn by
+    repeating the last (matlab/irc2.m:3669-3676).  numpy in, numpy out."""
+    vrKnn = np.asarray(vrKnn, np.float32)
+    with np.errstate(divide="ignore"):
+        rho = (np.float32(1.0) / vrKnn).astype(np.float32)
+    mi = np.asarray(viSpk_out, np.int64)[np.asarray(miKnn, np.int64) - 1]
+    if mi.shape[1] < knn:
+        mi = np.concatenate([mi, np.repeat(mi[:, -1:], knn - mi.shape[1], axis=1)], axis=1)
+    return rho, mi
+
+
+def delta_post(vrDelta_times_rho, viNneigh, viSpk_out):
+    """nneigh -> global id; NaN/Inf delta -> sqrt(SINGLE_INF) with nneigh set
+    to the spike's own local position (matlab/irc2.m:3720-3725, kept as is)."""
+    d = np.asarray(vrDelta_times_rho, np.float32).copy()
+    nn = np.asarray(viSpk_out, np.int64)[np.asarray(viNneigh, np.int64) - 1]
+    bad = np.flatnonzero(~np.isfinite(d))
+    nn[bad] = bad + 1
+    d[bad] = SQRT_SINGLE_INF_F
+    return d, nn
+
+
+def normalize_rho(vrRho):
+    """vrRho / max(vrRho); ordrho = sort(vrRho, 'descend') (matlab/irc2.m:3268-3269)."""
+    r = np.asarray(vrRho, np.float32)
+    r = (r / np.float32(np.nanmax(r))).astype(np.float32)
+    key = np.where(np.isnan(r), -np.inf, r)
+    ordrho = np.argsort(-key, kind="stable") + 1
+    return r, ordrho
+
+
+# ---------------------------------------------------------------------------
+# irc.m (v4) wrappers
+# ---------------------------------------------------------------------------
+
+def cuda_knn(mrFet, vi2, vi1, knn=30, nC_max=45):
+    """cuda_knn_ (matlab/irc.m:24365-24401): gathers B = mrFet(:,vi2),
+    A = mrFet(:,vi1) (0-based index vectors here), knn = min(knn, n2).
+    Returns vrKnn [n1], miKnn [n1, knn] mapped through vi2 (0-based)."""
+    if mrFet.shape[1] > nC_max:
+        raise ValueError("cuda_knn: nC > nC_max (the reference falls back to the CPU)")
+    vi2 = torch.as_tensor(vi2, device=mrFet.device, dtype=torch.long)
+    vi1 = torch.as_tensor(vi1, device=mrFet.device, dtype=torch.long)
+    knn = min(knn, vi2.numel())
+    K, I = cuda_knn_index(mrFet[vi2].contiguous(), mrFet[vi1].contiguous(), knn)
+    return K, vi2[I.long() - 1]
+
+
+def cuda_delta_knn_host(mrFet, vrRho, vi2, vi1):
+    """cuda_delta_knn_ (matlab/irc.m:24519-24553); returns D [n1] and N (0-based
+    through vi2; the reference's self-index fallback is an A-space index that
+    MATLAB also maps through vi2)."""
+    vi2 = torch.as_tensor(vi2, device=mrFet.device, dtype=torch.long)
+    vi1 = torch.as_tensor(vi1, device=mrFet.device, dtype=torch.long)
+    D, N = cuda_delta_knn(mrFet[vi2].contiguous(), mrFet[vi1].contiguous(),
+                          vrRho[vi2].contiguous(), vrRho[vi1].contiguous())
+    return D, vi2[N.long() - 1]
+
+
+def cuda_rho_drift(viSite1, viSite2, mrFet1, mrFet2, n1, dc2):
+    """cuda_rho_drift_ (matlab/irc.m:24612-24637) for one drift window of
+    n12 spikes (own chunk first, n1 of them)."""
+    site = torch.cat([torch.as_tensor(viSite1, dtype=torch.int32),
+                      torch.as_tensor(viSite2, dtype=torch.int32)]).to(mrFet1.device)
+    return rho_drift(site, mrFet1.contiguous(), mrFet2.contiguous(), n1, float(np.float32(dc2)))

@@ -1,0 +1,573 @@
+/*
+ * irc_oracle.c -- CPU oracle for the IronClust clustering hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
+ * calls this file; only the tests, the smoke check and the CPU-baseline leg of
+ * the benchmark use it, as the checker.
+ *
+ * Three groups of functions live here:
+ *
+ *  1. Restatements of the five reference CUDA kernels, one CPU loop nest per
+ *     kernel, following the per-thread scan order of the shipped sources so
+ *     that every float bit and every index matches:
+ *       orc_search_min_drift     matlab/search_min_drift.cu:24-94
+ *       orc_search_delta_drift   matlab/search_delta_drift.cu:24-106
+ *       orc_cuda_knn_index       matlab/cuda_knn_index.cu:27-111
+ *       orc_cuda_delta_knn       matlab/cuda_delta_knn.cu:19-87
+ *       orc_rho_drift            matlab/irc_cuda_rho_drift.cu:28-108
+ *     The kernels accumulate squared distances as `dist += d*d` with
+ *     d = b - a in feature order; nvcc contracts that into one fused
+ *     multiply-add per feature, which fmaf() restates.  This file must be
+ *     compiled with -ffp-contract=off so the C compiler adds no contraction of
+ *     its own.
+ *
+ *  2. The MATLAB post-processing the host applies to those outputs:
+ *       orc_post_sort_knn   `sort` (stable, NaN last) + first knn rows,
+ *                           matlab/irc2.m:3784-3787
+ *       orc_post_min        `min` along columns (first index, NaN skipped),
+ *                           matlab/irc2.m:3855-3857
+ *
+ *  3. Independent references:
+ *       orc_exact_knn_f64 / orc_exact_delta_f64
+ *            true k nearest neighbours / nearest higher-rho spike in double
+ *            precision over the same drift-linked candidate runs, ties broken
+ *            by (distance, index);
+ *       orc_knn_cpu / orc_delta_cpu
+ *            the reference's CPU path (irc2 with fGpu=0): knn_cpu_
+ *            (matlab/irc2.m:4244-4263, pdist2 'Smallest', self included) and
+ *            delta_cpu_ (matlab/irc2.m:3981-3994, expansion form, rho mask,
+ *            no zero-distance exclusion).  pdist2 and MATLAB's single BLAS
+ *            are closed, so their rounding is restated, not pinned.
+ *
+ * Array conventions follow MATLAB: features are column-major [nC x n]
+ * (the nC features of a spike are contiguous), 2-D outputs are
+ * column-major, returned indices are 1-based.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_SINGLE_INF ((float)3.402E+38)
+
+/* plan: per query chunk i, queries [q0[i], q0[i]+nq[i]) and candidate runs
+ * roff[i]..roff[i+1]-1 into (rs, rn): run start (0-based) and run length. */
+
+/* ------------------------------------------------------------------------ */
+/* 1. kernel restatements                                                    */
+/* ------------------------------------------------------------------------ */
+
+static inline float dist2_fma(const float *b, const float *a, int nC)
+{
+    float acc = 0.0f;
+    for (int c = 0; c < nC; ++c) {
+        float d = b[c] - a[c];
+        acc = fmaf(d, d, acc);
+    }
+    return acc;
+}
+
+/* search_min_drift.cu:24-94.  vnConst = {nC, nF, nBB, iA0, nA}; the launch
+ * (matlab/irc2.m:3775) covers every query of the chunk, wrapped blocks write
+ * identical values, so each query is evaluated once here.  D, I: [nT x nA]. */
+void orc_search_min_drift(float *D, int32_t *I, const float *F,
+                          const int32_t *IBB, const int32_t *NBB,
+                          const int32_t *vnConst, int nT)
+{
+    const int nC = vnConst[0], nBB = vnConst[2], iA0 = vnConst[3], nA = vnConst[4];
+    const int nT0 = nT / nBB;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int iA1 = 0; iA1 < nA; ++iA1) {
+        const int iA = iA0 + iA1;
+        const float *a = F + (size_t)iA * nC;
+        for (int tx = 0; tx < nT; ++tx) {
+            float tD = ORC_SINGLE_INF;
+            int tI = iA;
+            const int b = tx % nBB, iB0 = IBB[b], nB0 = NBB[b], iT0 = tx / nBB;
+            for (int iB = iT0 + iB0; iB < nB0 + iB0; iB += nT0) {
+                float d2 = dist2_fma(F + (size_t)iB * nC, a, nC);
+                if (d2 < tD && d2 > 0.0f) { tD = d2; tI = iB; }
+            }
+            D[tx + (size_t)nT * iA1] = sqrtf(tD < 0 ? -tD : tD);
+            I[tx + (size_t)nT * iA1] = tI + 1;
+        }
+    }
+}
+
+/* search_delta_drift.cu:24-106.  A candidate is masked when R[iB] <= R[iA]
+ * (so a NaN rho is NOT masked, as in the source). */
+void orc_search_delta_drift(float *D, int32_t *I, const float *F, const float *R,
+                            const int32_t *IBB, const int32_t *NBB,
+                            const int32_t *vnConst, int nT)
+{
+    const int nC = vnConst[0], nBB = vnConst[2], iA0 = vnConst[3], nA = vnConst[4];
+    const int nT0 = nT / nBB;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int iA1 = 0; iA1 < nA; ++iA1) {
+        const int iA = iA0 + iA1;
+        const float *a = F + (size_t)iA * nC;
+        const float ra = R[iA];
+        for (int tx = 0; tx < nT; ++tx) {
+            float tD = ORC_SINGLE_INF;
+            int tI = iA;
+            const int b = tx % nBB, iB0 = IBB[b], nB0 = NBB[b], iT0 = tx / nBB;
+            for (int iB = iT0 + iB0; iB < nB0 + iB0; iB += nT0) {
+                if (R[iB] <= ra) continue;          /* dist = SINGLE_INF + ... never wins */
+                float d2 = dist2_fma(F + (size_t)iB * nC, a, nC);
+                if (d2 < tD && d2 > 0.0f) { tD = d2; tI = iB; }
+            }
+            D[tx + (size_t)nT * iA1] = sqrtf(tD < 0 ? -tD : tD);
+            I[tx + (size_t)nT * iA1] = tI + 1;
+        }
+    }
+}
+
+/* cuda_knn_index.cu:27-111.  vnConst = {nB, nA, nC, knn}.  Per-thread
+ * minimum over iB = tx, tx+nT, ... (self kept), then the in-kernel selection
+ * sort with swaps (not stable), K = sqrt(|k-th|), I[knn x nA]. */
+void orc_cuda_knn_index(float *K, int32_t *I, const float *B, const float *A,
+                        const int32_t *vnConst, int nT)
+{
+    const int nB = vnConst[0], nA = vnConst[1], nC = vnConst[2], knn = vnConst[3];
+#pragma omp parallel
+    {
+        float *sD = (float *)malloc(sizeof(float) * nT);
+        int *sI = (int *)malloc(sizeof(int) * nT);
+#pragma omp for schedule(dynamic, 4)
+        for (int iA = 0; iA < nA; ++iA) {
+            const float *a = A + (size_t)iA * nC;
+            for (int t = 0; t < nT; ++t) { sD[t] = ORC_SINGLE_INF; sI[t] = 0; }
+            for (int tx = 0; tx < nT; ++tx)
+                for (int iB = tx; iB < nB; iB += nT) {
+                    float d2 = dist2_fma(B + (size_t)iB * nC, a, nC);
+                    if (d2 < sD[tx]) { sD[tx] = d2; sI[tx] = iB; }
+                }
+            for (int iK = 0; iK < knn; ++iK) {
+                float dmin = sD[iK];
+                int imin = iK;
+                for (int j = iK; j < nT; ++j)
+                    if (sD[j] < dmin) { dmin = sD[j]; imin = j; }
+                float tf = sD[imin]; sD[imin] = sD[iK]; sD[iK] = tf;
+                int ti = sI[imin]; sI[imin] = sI[iK]; sI[iK] = ti;
+            }
+            float v = sD[knn - 1];
+            K[iA] = sqrtf(v < 0 ? -v : v);
+            for (int iK = 0; iK < knn; ++iK) I[iK + (size_t)knn * iA] = sI[iK] + 1;
+        }
+        free(sD); free(sI);
+    }
+}
+
+/* cuda_delta_knn.cu:19-87.  vnConst = {nB, nA, nC}.  Candidate kept when
+ * R_B > R_A (strict; NaN excluded), zero distance kept, lowest thread slot
+ * wins ties, fallback index = iA (an A-space index, as in the source). */
+void orc_cuda_delta_knn(float *D, uint32_t *N, const float *B, const float *A,
+                        const float *R_B, const float *R_A, const int32_t *vnConst, int nT)
+{
+    const int nB = vnConst[0], nA = vnConst[1], nC = vnConst[2];
+#pragma omp parallel
+    {
+        float *sD = (float *)malloc(sizeof(float) * nT);
+        uint32_t *sN = (uint32_t *)malloc(sizeof(uint32_t) * nT);
+#pragma omp for schedule(dynamic, 4)
+        for (int iA = 0; iA < nA; ++iA) {
+            const float *a = A + (size_t)iA * nC;
+            const float ra = R_A[iA];
+            for (int t = 0; t < nT; ++t) { sD[t] = ORC_SINGLE_INF; sN[t] = 0; }
+            for (int tx = 0; tx < nT; ++tx)
+                for (int iB = tx; iB < nB; iB += nT) {
+                    float d2 = dist2_fma(B + (size_t)iB * nC, a, nC);
+                    if (R_B[iB] > ra && d2 < sD[tx]) { sD[tx] = d2; sN[tx] = (uint32_t)iB; }
+                }
+            float dmin = ORC_SINGLE_INF;
+            uint32_t imin = (uint32_t)iA;
+            for (int t = 0; t < nT; ++t)
+                if (sD[t] < dmin) { dmin = sD[t]; imin = sN[t]; }
+            D[iA] = sqrtf(dmin < 0 ? -dmin : dmin);
+            N[iA] = imin + 1;
+        }
+        free(sD); free(sN);
+    }
+}
+
+/* irc_cuda_rho_drift.cu:28-108.  vnConst = {n1, n12, nC}; miSite12 is
+ * [n12 x 2] column-major (primary, secondary site).  Distance = query minus
+ * candidate, fused per feature (calc_dist_, :18-25); counts are integers so
+ * the result does not depend on the scan order. */
+void orc_rho_drift(float *vrRho1, const int32_t *miSite12, const float *mrFet1,
+                   const float *mrFet2, const int32_t *vnConst, float dc2)
+{
+    const int n1 = vnConst[0], n12 = vnConst[1], nC = vnConst[2];
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i1 = 0; i1 < n1; ++i1) {
+        const int s = miSite12[i1];
+        const float *q = mrFet1 + (size_t)i1 * nC;
+        int nRho = 0, nComp = 0;
+        for (int j = 0; j < n12; ++j) {
+            const float *c;
+            if (miSite12[j] == s) c = mrFet1 + (size_t)j * nC;
+            else if (miSite12[j + n12] == s) c = mrFet2 + (size_t)j * nC;
+            else continue;
+            float acc = 0.0f;
+            for (int k = 0; k < nC; ++k) { float t = q[k] - c[k]; acc = fmaf(t, t, acc); }
+            if (acc <= dc2) ++nRho;
+            ++nComp;
+        }
+        vrRho1[i1] = (float)((double)nRho / (double)nComp);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 2. MATLAB post-processing                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* MATLAB `sort` ascending on single data: stable, NaN placed last. */
+static inline int mat_less(float x, int ix, float y, int iy)
+{
+    int nx = isnan(x), ny = isnan(y);
+    if (nx || ny) {
+        if (nx && ny) return ix < iy;
+        return ny;               /* non-NaN before NaN */
+    }
+    if (x < y) return 1;
+    if (y < x) return 0;
+    return ix < iy;
+}
+
+/* [vs, order] = sort(D); vrKnn = vs(knn,:); miKnn = I(order(1:knn,:))
+ * matlab/irc2.m:3784-3787.  D, I: [nT x nA]; outputs vrKnn [nA], miKnn [knn x nA]. */
+void orc_post_sort_knn(const float *D, const int32_t *I, int nT, int nA, int knn,
+                       float *vrKnn, int32_t *miKnn)
+{
+#pragma omp parallel
+    {
+        int *sel = (int *)malloc(sizeof(int) * (size_t)knn);
+#pragma omp for schedule(dynamic, 16)
+        for (int a = 0; a < nA; ++a) {
+            const float *col = D + (size_t)nT * a;
+            int n = 0;
+            /* partial insertion sort of the first knn in (value, position) order */
+            for (int t = 0; t < nT; ++t) {
+                if (n == knn && !mat_less(col[t], t, col[sel[n - 1]], sel[n - 1])) continue;
+                int p = (n < knn) ? n++ : n - 1;
+                while (p > 0 && mat_less(col[t], t, col[sel[p - 1]], sel[p - 1])) {
+                    sel[p] = sel[p - 1];
+                    --p;
+                }
+                sel[p] = t;
+            }
+            vrKnn[a] = col[sel[knn - 1]];
+            for (int k = 0; k < knn; ++k) miKnn[k + (size_t)knn * a] = I[sel[k] + (size_t)nT * a];
+        }
+        free(sel);
+    }
+}
+
+/* [vrMin, viMin] = min(D); viNneigh = I(viMin)   matlab/irc2.m:3855-3857 */
+void orc_post_min(const float *D, const int32_t *I, int nT, int nA,
+                  float *vrMin, int32_t *viNneigh)
+{
+    for (int a = 0; a < nA; ++a) {
+        const float *col = D + (size_t)nT * a;
+        int best = -1;
+        for (int t = 0; t < nT; ++t) {
+            if (isnan(col[t])) continue;
+            if (best < 0 || col[t] < col[best]) best = t;
+        }
+        if (best < 0) { vrMin[a] = NAN; best = 0; }
+        else vrMin[a] = col[best];
+        viNneigh[a] = I[best + (size_t)nT * a];
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3a. exact FP64 references over a drift plan                              */
+/* ------------------------------------------------------------------------ */
+
+static inline double dist2_f64(const float *b, const float *a, int nC)
+{
+    double acc = 0.0;
+    for (int c = 0; c < nC; ++c) {
+        double d = (double)b[c] - (double)a[c];
+        acc += d * d;
+    }
+    return acc;
+}
+
+/* Top-knn by (d2, index) for every query of every chunk.  exclude_zero=1
+ * drops candidates at distance exactly 0 (self and exact duplicates), as the
+ * irc2 GPU kernels do; 0 keeps them, as knn_cpu_ does.  Outputs, indexed by
+ * q - q_base: idx [knn x nOut] (1-based into F, 0 when fewer than knn
+ * candidates exist), d2 [knn x nOut] (NAN when missing). */
+void orc_exact_knn_f64(int32_t *idx, double *d2out, const float *F, int nC,
+                       const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                       const int32_t *rs, const int32_t *rn, int nChunks,
+                       int q_base, int knn, int exclude_zero)
+{
+    for (int ch = 0; ch < nChunks; ++ch) {
+#pragma omp parallel
+        {
+            double *bd = (double *)malloc(sizeof(double) * (size_t)knn);
+            int *bi = (int *)malloc(sizeof(int) * (size_t)knn);
+#pragma omp for schedule(dynamic, 8)
+            for (int qq = 0; qq < nq[ch]; ++qq) {
+                const int q = q0[ch] + qq;
+                const float *a = F + (size_t)q * nC;
+                int n = 0;
+                for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+                    for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
+                        double d = dist2_f64(F + (size_t)c * nC, a, nC);
+                        if (exclude_zero && d == 0.0) continue;
+                        if (n == knn && !(d < bd[n - 1] || (d == bd[n - 1] && c < bi[n - 1]))) continue;
+                        int p = (n < knn) ? n++ : n - 1;
+                        while (p > 0 && (d < bd[p - 1] || (d == bd[p - 1] && c < bi[p - 1]))) {
+                            bd[p] = bd[p - 1]; bi[p] = bi[p - 1]; --p;
+                        }
+                        bd[p] = d; bi[p] = c;
+                    }
+                const size_t o = (size_t)(q - q_base) * knn;
+                for (int k = 0; k < knn; ++k) {
+                    idx[o + k] = (k < n) ? bi[k] + 1 : 0;
+                    d2out[o + k] = (k < n) ? bd[k] : NAN;
+                }
+            }
+            free(bd); free(bi);
+        }
+    }
+}
+
+/* Nearest candidate with strictly higher rho (R indexed like F), distance > 0
+ * when exclude_zero, ties by (d2, index).  Outputs indexed by q - q_base:
+ * nn (1-based, 0 when none) and d2 (INFINITY when none). */
+void orc_exact_delta_f64(int32_t *nn, double *d2out, const float *F, const float *R, int nC,
+                         const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                         const int32_t *rs, const int32_t *rn, int nChunks,
+                         int q_base, int exclude_zero)
+{
+    for (int ch = 0; ch < nChunks; ++ch) {
+#pragma omp parallel for schedule(dynamic, 8)
+        for (int qq = 0; qq < nq[ch]; ++qq) {
+            const int q = q0[ch] + qq;
+            const float *a = F + (size_t)q * nC;
+            const float ra = R[q];
+            double best = INFINITY;
+            int bi = -1;
+            for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+                for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
+                    if (!(R[c] > ra)) continue;
+                    double d = dist2_f64(F + (size_t)c * nC, a, nC);
+                    if (exclude_zero && d == 0.0) continue;
+                    if (d < best || (d == best && c < bi)) { best = d; bi = c; }
+                }
+            nn[q - q_base] = bi + 1;
+            d2out[q - q_base] = best;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3b. the reference CPU path (irc2 fGpu=0), one call per drift chunk        */
+/* ------------------------------------------------------------------------ */
+
+/* knn_cpu_ (matlab/irc2.m:4244-4263): pdist2(B', A', 'euclidean',
+ * 'Smallest', knn), self included.  B = gathered candidates [nC x nB],
+ * A = queries [nC x nA].  Distances in single precision, sqrt of a plain
+ * (unfused) sum of squares; ties by candidate order.  Outputs vrKnn [nA]
+ * (k-th distance), miKnn [knn x nA] (1-based into B, padded by repeating
+ * the last row when nB < knn). */
+void orc_knn_cpu(float *vrKnn, int32_t *miKnn, const float *B, int nB,
+                 const float *A, int nA, int nC, int knn)
+{
+    const int kk = knn < nB ? knn : nB;
+#pragma omp parallel
+    {
+        float *bd = (float *)malloc(sizeof(float) * (size_t)(kk > 0 ? kk : 1));
+        int *bi = (int *)malloc(sizeof(int) * (size_t)(kk > 0 ? kk : 1));
+        float *dd = (float *)malloc(sizeof(float) * (size_t)(nB > 0 ? nB : 1));
+#pragma omp for schedule(dynamic, 4)
+        for (int ia = 0; ia < nA; ++ia) {
+            const float *a = A + (size_t)ia * nC;
+            for (int ib = 0; ib < nB; ++ib) {
+                const float *b = B + (size_t)ib * nC;
+                float s = 0.0f;
+                for (int c = 0; c < nC; ++c) { float d = a[c] - b[c]; s += d * d; }
+                dd[ib] = s;
+            }
+            int n = 0;
+            for (int ib = 0; ib < nB; ++ib) {
+                float d = dd[ib];
+                if (n == kk && !(d < bd[n - 1])) continue;
+                int p = (n < kk) ? n++ : n - 1;
+                while (p > 0 && d < bd[p - 1]) { bd[p] = bd[p - 1]; bi[p] = bi[p - 1]; --p; }
+                bd[p] = d; bi[p] = ib;
+            }
+            vrKnn[ia] = kk > 0 ? sqrtf(bd[kk - 1]) : NAN;
+            for (int k = 0; k < knn; ++k)
+                miKnn[k + (size_t)knn * ia] = kk > 0 ? bi[k < kk ? k : kk - 1] + 1 : 0;
+        }
+        free(bd); free(bi); free(dd);
+    }
+}
+
+/* delta_cpu_ (matlab/irc2.m:3981-3994): D = sum(y.^2) + (sum(x.^2)' - 2*x'*y),
+ * masked to inf where rho_x <= rho_y, [v, i] = min(D) (first index), then
+ * sqrt(abs(v)).  Zero distance is not excluded.  B = candidates [nC x nB]
+ * with rho RB, A = queries [nC x nA] with rho RA.  Outputs delta [nA],
+ * nneigh [nA] (1-based into B). */
+void orc_delta_cpu(float *delta, int32_t *nneigh, const float *B, const float *RB, int nB,
+                   const float *A, const float *RA, int nA, int nC)
+{
+    float *sx = (float *)malloc(sizeof(float) * (size_t)(nB > 0 ? nB : 1));
+    for (int ib = 0; ib < nB; ++ib) {
+        const float *b = B + (size_t)ib * nC;
+        float s = 0.0f;
+        for (int c = 0; c < nC; ++c) s += b[c] * b[c];
+        sx[ib] = s;
+    }
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int ia = 0; ia < nA; ++ia) {
+        const float *a = A + (size_t)ia * nC;
+        float sy = 0.0f;
+        for (int c = 0; c < nC; ++c) sy += a[c] * a[c];
+        const float ra = RA[ia];
+        float best = NAN;
+        int bi = 0;
+        for (int ib = 0; ib < nB; ++ib) {
+            const float *b = B + (size_t)ib * nC;
+            float g = 0.0f;
+            for (int c = 0; c < nC; ++c) g += b[c] * a[c];
+            float d = sy + (sx[ib] - 2.0f * g);
+            if (RB[ib] <= ra) d = INFINITY;
+            if (isnan(d)) continue;                 /* MATLAB min skips NaN */
+            if (isnan(best) || d < best) { best = d; bi = ib; }
+        }
+        delta[ia] = sqrtf(fabsf(best));
+        nneigh[ia] = bi + 1;
+    }
+    free(sx);
+}
+
+/* Drive knn_cpu_ / delta_cpu_ over a drift plan exactly as rho_paged_site_ /
+ * delta_paged_site_ do on their CPU branch (matlab/irc2.m:3653-3668,
+ * :3703-3719): per chunk, gather the linked runs, run the call, map indices
+ * back.  Outputs indexed by q - q_base; indices 1-based into F. */
+void orc_site_knn_cpu(float *vrKnn, int32_t *miKnn, const float *F, int nC,
+                      const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                      const int32_t *rs, const int32_t *rn, int nChunks, int q_base, int knn)
+{
+    for (int ch = 0; ch < nChunks; ++ch) {
+        int nB = 0;
+        for (int r = roff[ch]; r < roff[ch + 1]; ++r) nB += rn[r];
+        float *B = (float *)malloc(sizeof(float) * (size_t)nC * (nB > 0 ? nB : 1));
+        int32_t *map = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nB > 0 ? nB : 1));
+        int p = 0;
+        for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+            for (int c = rs[r]; c < rs[r] + rn[r]; ++c, ++p) {
+                memcpy(B + (size_t)p * nC, F + (size_t)c * nC, sizeof(float) * nC);
+                map[p] = c;
+            }
+        const int o = q0[ch] - q_base;
+        int32_t *mk = miKnn + (size_t)o * knn;
+        orc_knn_cpu(vrKnn + o, mk, B, nB, F + (size_t)q0[ch] * nC, nq[ch], nC, knn);
+        for (size_t i = 0; i < (size_t)knn * nq[ch]; ++i)
+            if (mk[i] > 0) mk[i] = map[mk[i] - 1] + 1;
+        free(B); free(map);
+    }
+}
+
+void orc_site_delta_cpu(float *delta, int32_t *nneigh, const float *F, const float *R, int nC,
+                        const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                        const int32_t *rs, const int32_t *rn, int nChunks, int q_base)
+{
+    for (int ch = 0; ch < nChunks; ++ch) {
+        int nB = 0;
+        for (int r = roff[ch]; r < roff[ch + 1]; ++r) nB += rn[r];
+        float *B = (float *)malloc(sizeof(float) * (size_t)nC * (nB > 0 ? nB : 1));
+        float *RB = (float *)malloc(sizeof(float) * (size_t)(nB > 0 ? nB : 1));
+        int32_t *map = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nB > 0 ? nB : 1));
+        int p = 0;
+        for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+            for (int c = rs[r]; c < rs[r] + rn[r]; ++c, ++p) {
+                memcpy(B + (size_t)p * nC, F + (size_t)c * nC, sizeof(float) * nC);
+                RB[p] = R[c];
+                map[p] = c;
+            }
+        const int o = q0[ch] - q_base;
+        orc_delta_cpu(delta + o, nneigh + o, B, RB, nB, F + (size_t)q0[ch] * nC,
+                      R + q0[ch], nq[ch], nC);
+        for (int i = 0; i < nq[ch]; ++i) nneigh[o + i] = map[nneigh[o + i] - 1] + 1;
+        free(B); free(RB); free(map);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3c. exact references in the reference FP32 arithmetic                     */
+/* ------------------------------------------------------------------------ */
+
+/* True top-knn under the reference FP32 distance (dist2_fma: d = b - a,
+ * fused accumulate in feature order), d2 > 0 and d2 < SINGLE_INF, ordered by
+ * (d2, index).  Missing entries: index = query + 1, d2 = SINGLE_INF.
+ * Outputs indexed by q - q_base: idx [knn x nOut] (1-based), d2 [knn x nOut]. */
+void orc_exact_knn_f32(int32_t *idx, float *d2out, const float *F, int nC,
+                       const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                       const int32_t *rs, const int32_t *rn, int nChunks, int q_base, int knn)
+{
+    for (int ch = 0; ch < nChunks; ++ch) {
+#pragma omp parallel
+        {
+            float *bd = (float *)malloc(sizeof(float) * (size_t)knn);
+            int *bi = (int *)malloc(sizeof(int) * (size_t)knn);
+#pragma omp for schedule(dynamic, 8)
+            for (int qq = 0; qq < nq[ch]; ++qq) {
+                const int q = q0[ch] + qq;
+                const float *a = F + (size_t)q * nC;
+                int n = 0;
+                for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+                    for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
+                        float d = dist2_fma(F + (size_t)c * nC, a, nC);
+                        if (!(d > 0.0f) || !(d < ORC_SINGLE_INF)) continue;
+                        if (n == knn && !(d < bd[n - 1] || (d == bd[n - 1] && c < bi[n - 1]))) continue;
+                        int p = (n < knn) ? n++ : n - 1;
+                        while (p > 0 && (d < bd[p - 1] || (d == bd[p - 1] && c < bi[p - 1]))) {
+                            bd[p] = bd[p - 1]; bi[p] = bi[p - 1]; --p;
+                        }
+                        bd[p] = d; bi[p] = c;
+                    }
+                const size_t o = (size_t)(q - q_base) * knn;
+                for (int k = 0; k < knn; ++k) {
+                    idx[o + k] = (k < n) ? bi[k] + 1 : q + 1;
+                    d2out[o + k] = (k < n) ? bd[k] : ORC_SINGLE_INF;
+                }
+            }
+            free(bd); free(bi);
+        }
+    }
+}
+
+/* Nearest candidate not masked by R[c] <= R[q] (the search_delta_drift
+ * mask), FP32 reference distance, d2 > 0 and < SINGLE_INF, ties by
+ * (d2, index).  Missing: nn = q + 1, d2 = SINGLE_INF.  Indexed by q - q_base. */
+void orc_exact_delta_f32(int32_t *nn, float *d2out, const float *F, const float *R, int nC,
+                         const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                         const int32_t *rs, const int32_t *rn, int nChunks, int q_base)
+{
+    for (int ch = 0; ch < nChunks; ++ch) {
+#pragma omp parallel for schedule(dynamic, 8)
+        for (int qq = 0; qq < nq[ch]; ++qq) {
+            const int q = q0[ch] + qq;
+            const float *a = F + (size_t)q * nC;
+            const float ra = R[q];
+            float best = ORC_SINGLE_INF;
+            int bi = -1;
+            for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+                for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
+                    if (R[c] <= ra) continue;
+                    float d = dist2_fma(F + (size_t)c * nC, a, nC);
+                    if (!(d > 0.0f) || !(d < ORC_SINGLE_INF)) continue;
+                    if (bi < 0 || d < best || (d == best && c < bi)) { best = d; bi = c; }
+                }
+            nn[q - q_base] = (bi < 0 ? q : bi) + 1;
+            d2out[q - q_base] = best;
+        }
+    }
+}

@@ -1,0 +1,118 @@
+"""Drop-in kernels vs the reference's own kernels (and the CPU oracle).
+
+Every comparison is bit-exact: float outputs are compared as raw bits.
+The reference kernels are the shipped .cu sources compiled to PTX and
+launched with the MATLAB launch configuration (oracle/ref_harness.cu).
+"""
+import numpy as np
+import pytest
+import torch
+
+from ironclust_gb300 import irc
+from oracle import oracle as O
+from tests.cases import rho_with_ties, small_site
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(t):
+    a = t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
+    return a.view(np.int32) if a.dtype == np.float32 else a
+
+
+def same(a, b):
+    return np.array_equal(bits(a), bits(b))
+
+
+CASES = [
+    dict(n=3000, d=24, n_chunks=5, seed=7),
+    dict(n=2500, d=33, n_chunks=4, seed=8, secondary=True),
+    dict(n=1203, d=45, n_chunks=3, seed=9, sizes=[1, 601, 601]),
+]
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("nT", [1024, 512])
+def test_search_min_drift_bitexact(gpu, refk, case, nT):
+    F, plan, _ = small_site(**case)
+    Fd = torch.from_numpy(F).to(gpu)
+    for i in range(len(plan["q0"])):
+        r0, r1 = plan["roff"][i], plan["roff"][i + 1]
+        IBB = torch.from_numpy(plan["rs"][r0:r1]).to(gpu)
+        NBB = torch.from_numpy(plan["rn"][r0:r1]).to(gpu)
+        vn = [F.shape[1], F.shape[0], int(r1 - r0), int(plan["q0"][i]), int(plan["nq"][i])]
+        D, I = irc.search_min_drift(Fd, IBB, NBB, vn, nThreads=nT)
+        Dr, Ir = refk.search_min_drift(Fd, IBB, NBB, vn, nT=nT)
+        assert same(D, Dr) and same(I, Ir), "chunk %d differs from the reference kernel" % i
+        if i == 0:
+            Do, Io = O.search_min_drift(F, plan["rs"][r0:r1], plan["rn"][r0:r1], vn, nT)
+            assert same(D, Do) and same(I, Io), "oracle differs"
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_search_delta_drift_bitexact(gpu, refk, case):
+    F, plan, _ = small_site(**case)
+    R = rho_with_ties(F.shape[0])
+    Fd, Rd = torch.from_numpy(F).to(gpu), torch.from_numpy(R).to(gpu)
+    for i in range(len(plan["q0"])):
+        r0, r1 = plan["roff"][i], plan["roff"][i + 1]
+        IBB = torch.from_numpy(plan["rs"][r0:r1]).to(gpu)
+        NBB = torch.from_numpy(plan["rn"][r0:r1]).to(gpu)
+        vn = [F.shape[1], F.shape[0], int(r1 - r0), int(plan["q0"][i]), int(plan["nq"][i])]
+        D, I = irc.search_delta_drift(Fd, Rd, IBB, NBB, vn)
+        Dr, Ir = refk.search_delta_drift(Fd, Rd, IBB, NBB, vn)
+        assert same(D, Dr) and same(I, Ir), "chunk %d differs" % i
+        if i == 0:
+            Do, Io = O.search_delta_drift(F, R, plan["rs"][r0:r1], plan["rn"][r0:r1], vn)
+            assert same(D, Do) and same(I, Io)
+
+
+@pytest.mark.parametrize("nB,nA,nC,knn", [(1500, 200, 33, 30), (300, 77, 24, 30), (40, 17, 18, 40),
+                                          (5000, 33, 60, 30)])
+def test_cuda_knn_index_bitexact(gpu, refk, nB, nA, nC, knn):
+    rng = np.random.default_rng(nB + nA)
+    B = rng.normal(0, 3, (nB, nC)).astype(np.float32)
+    B[5] = B[4]                                                   # duplicate candidates
+    A = np.concatenate([B[:nA // 2], rng.normal(0, 3, (nA - nA // 2, nC))]).astype(np.float32)
+    knn = min(knn, nB)
+    Bd, Ad = torch.from_numpy(B).to(gpu), torch.from_numpy(A).to(gpu)
+    K, I = irc.cuda_knn_index(Bd, Ad, knn)
+    Kr, Ir = refk.cuda_knn_index(Bd, Ad, knn)
+    assert same(K, Kr) and same(I, Ir)
+    Ko, Io = O.cuda_knn_index(B, A, knn)
+    assert same(K, Ko) and same(I, Io)
+
+
+@pytest.mark.parametrize("nB,nA,nC", [(1500, 200, 33), (100, 300, 24), (3000, 16, 45)])
+def test_cuda_delta_knn_bitexact(gpu, refk, nB, nA, nC):
+    rng = np.random.default_rng(nB * 3 + nA)
+    B = rng.normal(0, 3, (nB, nC)).astype(np.float32)
+    A = B[rng.choice(nB, nA)] if nA <= nB else rng.normal(0, 3, (nA, nC)).astype(np.float32)
+    RB = rho_with_ties(nB, 5)
+    RA = rho_with_ties(nA, 6)
+    RA[0] = RB.max() + 1                     # a query with no higher-rho candidate
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(gpu)
+    D, N = irc.cuda_delta_knn(t(B), t(A), t(RB), t(RA))
+    Dr, Nr = refk.cuda_delta_knn(t(B), t(A), t(RB), t(RA))
+    assert same(D, Dr) and same(N, Nr)
+    Do, No = O.cuda_delta_knn(B, A, RB, RA)
+    assert same(D, Do) and np.array_equal(N.cpu().numpy().view(np.uint32), No)
+
+
+@pytest.mark.parametrize("n12,n1,nC", [(1500, 300, 33), (700, 700, 24), (2000, 17, 45)])
+def test_rho_drift_bitexact(gpu, refk, n12, n1, nC):
+    rng = np.random.default_rng(n12 + n1)
+    f1 = rng.normal(0, 2, (n12, nC)).astype(np.float32)
+    f2 = (f1 + rng.normal(0, 0.5, (n12, nC))).astype(np.float32)
+    s1 = rng.integers(1, 4, n12).astype(np.int32)
+    s2 = rng.integers(1, 4, n12).astype(np.int32)
+    site = np.stack([s1, s2], 1)
+    d = ((f1[:50, None, :] - f1[None, :50, :]) ** 2).sum(-1)
+    dc2 = float(np.float32(np.quantile(d[d > 0], 0.2)))
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(gpu)
+    site_cm = t(np.concatenate([s1, s2]))
+    rho = irc.rho_drift(site_cm, t(f1), t(f2), n1, dc2)
+    rr = refk.rho_drift(site_cm, t(f1), t(f2), n1, dc2)
+    assert same(rho, rr)
+    ro = O.rho_drift(site, f1, f2, n1, dc2)
+    assert same(rho, ro)
