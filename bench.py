@@ -1,0 +1,398 @@
+"""Benchmark of the clustering hot path: kNN + rho + delta spikes/s.
+
+One step = the whole hot path (kNN over the drift-linked candidates, rho =
+1/d_knn, delta + nearest higher-rho spike) over one site of the
+``drift400k`` workload: 400,000 spikes, 33 features, 16 Gaussian clusters,
+200 drift chunks of ~2,000 spikes with a random-walk drift, each chunk
+linked to its 15 most similar chunks within +/-64, knn = 30 (seeded
+synthetic data: the recorded SpikeForest probes the reference measures on
+are not available).
+
+value : spikes/s of the headline form (inputs resident in HBM, L2 flushed
+        before every timed step, CUDA events on the launching stream).
+e2e   : the same through the public API with host buffers: H2D copy of the
+        features from pinned memory + the site call + D2H copy of rho, delta,
+        nneigh and the kNN list, every step.
+forms : spikes/s of every form measured in the same run (the plain FP32
+        drop-in "ref" form is the reference kernels' semantics bit for bit).
+
+Multi-GPU: every rank runs an independent site (sites shard with no
+exchange), value = all ranks' spikes / max-over-ranks time ("weak").
+
+--impl reference: the reference's CPU path (knn_cpu_ + delta_cpu_, irc2
+with fGpu=0) restated in C with OpenMP, all host cores, on a bounded sample
+of query chunks of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "kNN+rho+delta spikes/s: BF16-TC vs FP32 form on one GB300 at >=99.9% kNN recall"
+WORKLOAD = "drift400k"
+KNN = 30
+
+
+def _dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return dict(hbm=p["hbm_gbs"], bf16=p["bf16_tflops"], bf16_sus=p["bf16_tflops_sustained"],
+                    src="measured")
+    except Exception:
+        return dict(hbm=6800.0, bf16=1900.0, bf16_sus=1700.0, src="fallback")
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(rank, scale):
+    from ironclust_gb300 import synth
+    site = synth.make_workload(WORKLOAD, scale=scale, seed_offset=rank)
+    plan = synth.site_plan(site)
+    return site, plan
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from ironclust_gb300 import _lib, build, irc
+    from ironclust_gb300.drift import plan_pairs
+
+    rank, world, local = _dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    build.build()
+    _lib.lib()
+    site, plan = make_inputs(rank, args.scale)
+    N, D = site["F"].shape
+    pairs = plan_pairs(plan)
+    F = torch.from_numpy(site["F"]).to(dev)
+    P = irc.Plan(plan)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)     # > L2 (126 MB)
+    stream = torch.cuda.current_stream()
+
+    forms = [m.strip() for m in args.forms.split(",") if m.strip()]
+    head = args.mode if args.mode in forms else forms[0]
+    results = {}
+    kernel_ms = {}
+    for mode in forms:
+        def step():
+            return irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
+        try:
+            for _ in range(args.warmup):
+                step()
+            torch.cuda.synchronize()
+        except _lib.IrcError as e:
+            results[mode] = {"error": str(e)}
+            continue
+        times = []
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(dev.index) as cs:
+            for _ in range(args.steps):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step()
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        ms = sum(times) / len(times)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        results[mode] = {"spikes_per_s": world * N / (ms / 1e3), "ms_per_step": ms,
+                         "clocks": cs.summary()}
+        kernel_ms[mode] = time_kernels(P, F, mode, stream, flush, torch, irc)
+
+    # accuracy of the headline form against the FP64 oracle is measured in the
+    # tests; here the recall of each form is checked against the EXACT form
+    # (whose kNN equals the FP32 oracle bit for bit) on the full workload.
+    recall = {}
+    if "exact" in forms and not results.get("exact", {}).get("error"):
+        ref = irc.site_knn(P, F, KNN, "exact")["miKnn"]
+        for mode in forms:
+            if mode in ("exact",) or results.get(mode, {}).get("error"):
+                continue
+            got = irc.site_knn(P, F, KNN, mode)["miKnn"]
+            recall[mode] = knn_recall(ref, got, torch)
+
+    # end-to-end through host buffers (headline form)
+    e2e = None
+    if not results.get(head, {}).get("error"):
+        e2e = time_e2e(P, site["F"], head, args, dev, torch, irc, world, dist if world > 1 else None)
+
+    out = None
+    if rank == 0:
+        peaks = _peaks()
+        hr = results.get(head, {})
+        km = kernel_ms.get(head, {})
+        dom_name, dom_ms = (max(km.items(), key=lambda kv: kv[1]) if km else (None, None))
+        flops = 2.0 * D * pairs
+        roof = None
+        if dom_ms:
+            if head in ("bf16", "fp8"):
+                ach = flops / (dom_ms / 1e3) / 1e12
+                roof = {"bound": "tensor", "kernel": dom_name, "achieved": ach, "peak": peaks["bf16"],
+                        "unit": "TFLOP/s", "frac": ach / peaks["bf16"], "traffic": None,
+                        "peak_src": peaks["src"] + " bf16 burst"}
+            else:
+                ach = flops / (dom_ms / 1e3) / 1e12
+                fp32_peak = 2 * 128 * 152 * 2.07e9 / 1e12        # FP32 SIMT FMA, nominal
+                roof = {"bound": "fp32-simt", "kernel": dom_name, "achieved": ach, "peak": fp32_peak,
+                        "unit": "TFLOP/s", "frac": ach / fp32_peak, "traffic": None,
+                        "peak_src": "nominal 152 SM x 128 lanes x 2.07 GHz"}
+        n_launch = {"ref": 2, "exact": 4, "bf16": 5, "fp8": 5}
+        out = {
+            "metric": METRIC, "value": hr.get("spikes_per_s"), "unit": "spikes/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": hr.get("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"bf16": "bf16", "fp8": "fp8-e4m3", "exact": "f32", "ref": "f32"}.get(head, "f32"),
+            "data": "synthetic (seeded Gaussian clusters + 5% noise, random-walk drift)",
+            "config": {"workload": WORKLOAD, "spikes_per_site": N, "features": D, "chunks": len(plan["q0"]),
+                       "links_per_chunk": 15, "knn": KNN, "form": head, "pairs": pairs,
+                       "parallelism": "sites sharded over ranks" if world > 1 else "single site",
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "forms": {m: {k: v for k, v in r.items() if k != "clocks"} for m, r in results.items()},
+            "kernel_ms": kernel_ms,
+            "recall_vs_exact": recall,
+            "clocks": hr.get("clocks"),
+            "e2e": e2e,
+            "roofline": roof,
+            "gpu_launches": n_launch.get(head, 0) * args.steps,
+        }
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(site, plan, seconds=args.cpu_seconds)
+    P.close()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def knn_recall(ref, got, torch):
+    r = ref.long()
+    g = got.long()
+    n = r.shape[0]
+    hits = 0
+    for s in range(0, n, 65536):
+        a = r[s:s + 65536]
+        b = g[s:s + 65536]
+        hits += (a.unsqueeze(2) == b.unsqueeze(1)).any(2).sum().item()
+    return hits / float(r.numel())
+
+
+def time_kernels(P, F, mode, stream, flush, torch, irc):
+    """Per-phase device times of one step (CUDA events on the launch stream)."""
+    flush.zero_()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(stream)
+    k = irc.site_knn(P, F, KNN, mode)
+    ev[1].record(stream)
+    irc.site_delta(P, F, k["rho"], mode, 512, KNN, k["miKnn"], k["d2Knn"])
+    ev[2].record(stream)
+    ev[2].synchronize()
+    return {"knn": ev[0].elapsed_time(ev[1]), "delta": ev[1].elapsed_time(ev[2])}
+
+
+def time_e2e(P, F_host, mode, args, dev, torch, irc, world, dist):
+    Fh = torch.from_numpy(F_host).pin_memory()
+    N = Fh.shape[0]
+    Fd = torch.empty_like(Fh, device=dev)
+    outs = {"rho": torch.empty(N, dtype=torch.float32).pin_memory(),
+            "delta": torch.empty(N, dtype=torch.float32).pin_memory(),
+            "nneigh": torch.empty(N, dtype=torch.int32).pin_memory(),
+            "miKnn": torch.empty((N, KNN), dtype=torch.int32).pin_memory()}
+    stream = torch.cuda.current_stream()
+
+    def step():
+        Fd.copy_(Fh, non_blocking=True)
+        r = irc.knn_rho_delta_site(P, Fd, knn=KNN, mode=mode)
+        for k, h in outs.items():
+            h.copy_(r[k], non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    h2d = Fh.numel() * 4
+    d2h = sum(h.numel() * h.element_size() for h in outs.values())
+    return {"value": world * N / (ms / 1e3), "unit": "spikes/s", "ms_per_step": ms,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+
+def cpu_baseline(site, plan, seconds=15.0, chunks=None):
+    """The reference CPU path (knn_cpu_ + delta_cpu_, OpenMP, all host cores)
+    over a bounded sample of query chunks; spikes/s of the sample."""
+    from oracle import oracle as O
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    F = site["F"]
+    rng = np.random.default_rng(0)
+    R_stand_in = rng.uniform(0.05, 1.0, F.shape[0]).astype(np.float32)
+    n_done, t_used, n_ch = 0, 0.0, 0
+    n_total = len(plan["q0"])
+    step = 1 if chunks is None else chunks
+    while n_ch < n_total:
+        take = min(step, n_total - n_ch)
+        # the next `take` query chunks, with their own candidate runs
+        new = dict(q0=plan["q0"][n_ch:n_ch + take], nq=plan["nq"][n_ch:n_ch + take],
+                   roff=(plan["roff"][n_ch:n_ch + take + 1] - plan["roff"][n_ch]),
+                   rs=plan["rs"][plan["roff"][n_ch]:plan["roff"][n_ch + take]],
+                   rn=plan["rn"][plan["roff"][n_ch]:plan["roff"][n_ch + take]],
+                   q_base=int(plan["q0"][n_ch]), n_out=int(plan["nq"][n_ch:n_ch + take].sum()),
+                   n_f=plan["n_f"])
+        t0 = time.perf_counter()
+        vr, _ = O.site_knn_cpu(F, new, KNN)
+        R = R_stand_in.copy()
+        R[new["q_base"]:new["q_base"] + new["n_out"]] = 1.0 / vr
+        O.site_delta_cpu(F, R, new)
+        t_used += time.perf_counter() - t0
+        n_done += new["n_out"]
+        n_ch += take
+        if chunks is None and t_used >= seconds:
+            break
+        if chunks is not None:
+            break
+    return {"value": n_done / t_used, "unit": "spikes/s", "cores": cores, "kind": "port",
+            "sample": "%d query chunks (%d of %d spikes) of %s through knn_cpu_ + delta_cpu_ (C port, "
+                      "OpenMP); rho of non-sampled candidates is a seeded stand-in" % (
+                          n_ch, n_done, site["F"].shape[0], WORKLOAD),
+            "seconds": t_used}
+
+
+def run_reference(args):
+    rank, world, _ = _dist_env()
+    if rank != 0:
+        return None
+    site, plan = make_inputs(0, args.scale)
+    N = site["F"].shape[0]
+    from oracle import oracle as O  # noqa: F401  (builds the oracle library)
+    sample_chunks = args.ref_chunks
+    for _ in range(args.warmup):
+        cpu_baseline(site, plan, chunks=sample_chunks)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(site, plan, chunks=sample_chunks))
+    wall = time.perf_counter() - t0
+    v = sum(x["value"] for x in vals) / len(vals)
+    return {"metric": METRIC, "value": v, "unit": "spikes/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
+            "data": "synthetic (seeded Gaussian clusters + 5% noise, random-walk drift)",
+            "config": {"workload": WORKLOAD, "spikes_per_site": N, "knn": KNN,
+                       "form": "reference CPU path (irc2 fGpu=0): knn_cpu_ + delta_cpu_"},
+            "cpu_baseline": {k: vals[0][k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "spikes/s"},
+            "e2e": {"value": v, "unit": "spikes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="bf16")
+    ap.add_argument("--forms", default="bf16,exact,ref")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-chunks", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -111,6 +111,12 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
                     int nF);
 int irc_plan_destroy(irc_plan *plan);
 
+/* Synchronises `stream` and reports IRC_E_TIMEOUT if a bounded device-side
+ * wait in one of the plan's kernels gave up since the last check (the
+ * kernel then returned early and its outputs are incomplete); clears the
+ * flag.  No reference counterpart: the reference kernels have no waits. */
+int irc_plan_check(irc_plan *plan, void *stream);
+
 /* kNN + rho of every query of the plan (rho_paged_site_ up to the global-id
  * mapping, matlab/irc2.m:3645-3670).
  * vrKnn [n_out]: distance of the knn-th neighbour; rho [n_out] (optional) =

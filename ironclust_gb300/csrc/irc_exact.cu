@@ -330,8 +330,8 @@ __global__ void k_delta_scan(irc::PlanDev p, const float *__restrict__ F, const 
 static int irc_plan_scratch(irc_plan *pl, int **counters, int **list_a, int **list_b)
 {
     *counters = pl->scratch;
-    *list_a = pl->scratch + 2;
-    *list_b = pl->scratch + 2 + pl->dev.n_out;
+    *list_a = pl->scratch + irc::kScratchLists;
+    *list_b = pl->scratch + irc::kScratchLists + pl->dev.n_out;
     return IRC_OK;
 }
 

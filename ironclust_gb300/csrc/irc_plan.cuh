@@ -4,6 +4,12 @@
 
 namespace irc {
 
+// Plan scratch words: [0] overflow-queue count, [1] delta-fallback count,
+// [2] device error word (a bounded wait gave up), [3] unused; the two query
+// lists of n_out entries follow.
+constexpr int kScratchErr = 2;
+constexpr int kScratchLists = 4;
+
 // Query-tile sizes for which a plan precomputes its tile tables.
 constexpr int kTileSizes[] = {8, 16, 32, 64, 128};
 constexpr int kNumTileSizes = 5;
@@ -41,7 +47,9 @@ __device__ __forceinline__ void tile_lookup(const PlanDev &p, int tile, int &chu
 struct irc_plan {
     irc::PlanDev dev;
     void *dmem;                            // single device allocation behind dev
-    int32_t *scratch;                      // inside dmem: 2 counters + 2 x n_out query lists
+    int32_t *scratch;                      // inside dmem: 4 words + 2 x n_out query lists
+    void *tc_buf;                          // tensor-core operand rows (2 x nF x tc_row_bytes), lazily
+    size_t tc_row_bytes;
     int ntiles[irc::kNumTileSizes];        // host copy of tile counts
     int max_nq;                            // largest query chunk
     long long pairs;                       // (query, candidate) pairs of the plan

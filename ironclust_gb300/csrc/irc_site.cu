@@ -149,6 +149,23 @@ inline int tiles_for(const irc_plan *pl, int qb) { return pl->ntiles[irc::tile_s
 
 }  // namespace
 
+// Tensor-core operand rows: two [nF x row_bytes] matrices, allocated on the
+// first tensor-core call of a plan and kept until irc_plan_destroy.
+int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, size_t row_bytes)
+{
+    const size_t one = (size_t)pl->dev.nF * row_bytes;
+    if (!pl->tc_buf || pl->tc_row_bytes != row_bytes) {
+        if (pl->tc_buf) cudaFree(pl->tc_buf);
+        pl->tc_buf = nullptr;
+        cudaError_t e = cudaMalloc(&pl->tc_buf, 2 * one);
+        if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn: operand buffers");
+        pl->tc_row_bytes = row_bytes;
+    }
+    *fq = pl->tc_buf;
+    *fc = (char *)pl->tc_buf + one;
+    return IRC_OK;
+}
+
 int irc_exact_chunk_fill(float *, int32_t *, const float *, const int32_t *, const int32_t *, int,
                          int, int, int, int, int, cudaStream_t)
 {
@@ -228,7 +245,7 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
         pl->ntiles[k] = acc;
     }
     cudaGetDevice(&pl->device);
-    const size_t scratch_ints = 2 + 2 * (size_t)n_out;
+    const size_t scratch_ints = irc::kScratchLists + 2 * (size_t)n_out;
     cudaError_t e = cudaMalloc(&pl->dmem, (img.size() + scratch_ints) * sizeof(int32_t));
     if (e != cudaSuccess) {
         free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn); free(pl);
@@ -260,9 +277,26 @@ int irc_plan_destroy(irc_plan *pl)
 {
     if (!pl) return IRC_OK;
     cudaError_t e = cudaFree(pl->dmem);
+    if (pl->tc_buf) cudaFree(pl->tc_buf);
     free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn);
     free(pl);
     return e == cudaSuccess ? IRC_OK : irc_host::cuda_status(e, "irc_plan_destroy");
+}
+
+int irc_plan_check(irc_plan *pl, void *stream)
+{
+    if (!pl) { irc_host::set_error("irc_plan_check: null plan"); return IRC_E_INVAL; }
+    int word = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(&word, pl->scratch + irc::kScratchErr, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_plan_check");
+    if (word) {
+        cudaMemsetAsync(pl->scratch + irc::kScratchErr, 0, sizeof(int), s);
+        irc_host::set_error("a device-side wait of the plan's kernels timed out");
+        return IRC_E_TIMEOUT;
+    }
+    return IRC_OK;
 }
 
 int irc_site_knn(irc_plan *pl, const float *F, int nC, int knn, int nThreads, int mode,

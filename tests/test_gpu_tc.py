@@ -1,0 +1,79 @@
+"""Tensor-core (tcgen05 BF16) form vs the exact FP32 form and the FP64 oracle.
+
+Tolerances (the precision targets of the tensor-core form):
+  * kNN recall >= 0.999 against the FP64 oracle (set overlap of the k lists);
+  * rho = 1/d_knn within 1e-4 relative of the FP64 value;
+  * delta within 1e-4 relative of the FP64 value for spikes whose nearest
+    higher-rho neighbour agrees.
+Where the BF16 filter kept the true neighbours, the re-ranked lists equal the
+exact FP32 form bit for bit (same arithmetic), which is checked too.
+"""
+import numpy as np
+import pytest
+import torch
+
+from ironclust_gb300 import _lib, irc
+from oracle import oracle as O
+from tests.cases import small_site
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    dict(n=3000, d=24, n_chunks=5, seed=7),
+    dict(n=2500, d=33, n_chunks=4, seed=8, secondary=True),
+    dict(n=1203, d=45, n_chunks=3, seed=9, sizes=[1, 601, 601]),
+    dict(n=6000, d=18, n_chunks=1, seed=10),
+    dict(n=20000, d=33, n_chunks=10, seed=12),
+]
+
+
+def recall(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.mean([len(set(x) & set(y)) / len(x) for x, y in zip(a, b)])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_bf16_knn_matches_exact(gpu, case):
+    F, plan, _ = small_site(**case)
+    Fd = torch.from_numpy(F).to(gpu)
+    P = irc.Plan(plan)
+    tc = irc.site_knn(P, Fd, knn=30, mode="bf16")
+    ex = irc.site_knn(P, Fd, knn=30, mode="exact")
+    _lib.check(_lib.lib().irc_plan_check(P.h, irc._stream()), "irc_plan_check")
+    mt, me = tc["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy()
+    r = recall(mt, me)
+    assert r >= 0.999, r
+    same_rows = np.all(mt == me, axis=1)
+    assert same_rows.mean() >= 0.99
+    d2t, d2e = tc["d2Knn"].cpu().numpy(), ex["d2Knn"].cpu().numpy()
+    assert np.array_equal(d2t[same_rows].view(np.int32), d2e[same_rows].view(np.int32))
+    # against FP64 ground truth
+    i64, d64 = O.exact_knn_f64(F, plan, 30)
+    assert recall(mt, i64) >= 0.999
+    ok = np.isfinite(d64[:, 29])
+    rho64 = 1.0 / np.sqrt(d64[ok, 29])
+    rel = np.abs(tc["rho"].cpu().numpy()[ok] - rho64) / rho64
+    assert rel.max() <= 1e-4, rel.max()
+
+
+@pytest.mark.parametrize("case", CASES[:3] + CASES[4:])
+def test_bf16_delta_vs_fp64(gpu, case):
+    F, plan, _ = small_site(**case)
+    if plan["n_out"] != F.shape[0]:
+        pytest.skip("single-page site needed")
+    Fd = torch.from_numpy(F).to(gpu)
+    P = irc.Plan(plan)
+    out = irc.knn_rho_delta_site(P, Fd, knn=30, mode="bf16")
+    _lib.check(_lib.lib().irc_plan_check(P.h, irc._stream()), "irc_plan_check")
+    R = out["rho"].cpu().numpy()
+    nn32, d2_32 = O.exact_delta_f32(F, R, plan)
+    assert np.mean(out["nneigh"].cpu().numpy() == nn32) >= 0.999
+    nn64, d2_64 = O.exact_delta_f64(F, R, plan)
+    agree = out["nneigh"].cpu().numpy() == nn64
+    found = np.isfinite(d2_64)
+    de = out["delta"].cpu().numpy()
+    ref = np.sqrt(d2_64) * R
+    m = agree & found
+    rel = np.abs(de[m] - ref[m]) / ref[m]
+    assert rel.max() <= 1e-4
