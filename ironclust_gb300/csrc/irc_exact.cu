@@ -374,3 +374,15 @@ int irc_site_delta_list(irc_plan *pl, const float *F, int nC, const float *R, in
     IRC_CHECK_LAUNCH("irc_site_delta scan");
     return IRC_OK;
 }
+
+// Finish the queries the tensor-core kernel queued (list overflow) with the
+// exact ordered-scan kernel; the queue is the plan's first scratch list.
+int irc_exact_overflow_drain(irc_plan *pl, const float *F, int nC, int knn, float *vrKnn, float *rho,
+                             int32_t *miKnn, float *d2Knn, cudaStream_t s)
+{
+    int *cnt, *la, *lb;
+    irc_plan_scratch(pl, &cnt, &la, &lb);
+    k_exact_overflow<<<kQueueBlocks, 256, 0, s>>>(pl->dev, F, nC, knn, cnt, la, vrKnn, rho, miKnn, d2Knn);
+    IRC_CHECK_LAUNCH("irc_site_knn overflow drain");
+    return IRC_OK;
+}

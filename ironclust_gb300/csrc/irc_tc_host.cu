@@ -1,0 +1,128 @@
+// irc_tc_host.cu -- operand preparation and launch of the tensor-core kNN.
+//
+// Operand rows.  Every spike is stored twice in BF16, padded to K = 64 (one
+// 128-byte swizzle row):
+//     query row     [ -2*a_1 .. -2*a_D,  na_h, na_m, na_l,  1, 1, 1,  0 ... ]
+//     candidate row [    b_1 ..    b_D,     1,    1,    1, nb_h, nb_m, nb_l, 0 ... ]
+// where a, b are the BF16-rounded features and na = |a|^2 (FP32, from the
+// rounded values) split exactly into three BF16 terms, so one K = 64
+// contraction yields |a|^2 + |b|^2 - 2 a.b = |a - b|^2 of the rounded
+// features, accumulated in FP32.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include "irc_common.cuh"
+#include "irc_plan.cuh"
+#include "irc_tc.cuh"
+
+namespace {
+
+// F (f32 [nF x nC]) -> query / candidate BF16 rows of 64.
+__global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, uint4 *__restrict__ Fq,
+                            uint4 *__restrict__ Fc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nF) return;
+    const float *a = F + (size_t)i * nC;
+    float na = 0.0f;
+    for (int k = 0; k < nC; ++k) {
+        const float f = __bfloat162float(__float2bfloat16_rn(__ldg(a + k)));
+        na = __fmaf_rn(f, f, na);
+    }
+    const __nv_bfloat16 h = __float2bfloat16_rn(na);
+    const float rem1 = na - __bfloat162float(h);
+    const __nv_bfloat16 m = __float2bfloat16_rn(rem1);
+    const __nv_bfloat16 l = __float2bfloat16_rn(rem1 - __bfloat162float(m));
+    const __nv_bfloat16 one = __float2bfloat16_rn(1.0f), zero = __float2bfloat16_rn(0.0f);
+#pragma unroll 1
+    for (int j = 0; j < irc_tc::KP / 8; ++j) {
+        __align__(16) __nv_bfloat16 wq[8], wc[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int k = j * 8 + e;
+            __nv_bfloat16 vq = zero, vc = zero;
+            if (k < nC) {
+                const __nv_bfloat16 bf = __float2bfloat16_rn(__ldg(a + k));
+                vc = bf;
+                vq = __float2bfloat16_rn(-2.0f * __bfloat162float(bf));
+            } else if (k < nC + 3) {
+                vq = (k == nC) ? h : (k == nC + 1) ? m : l;
+                vc = one;
+            } else if (k < nC + 6) {
+                vq = one;
+                vc = (k == nC + 3) ? h : (k == nC + 4) ? m : l;
+            }
+            wq[e] = vq;
+            wc[e] = vc;
+        }
+        Fq[(size_t)i * (irc_tc::KP / 8) + j] = *reinterpret_cast<uint4 *>(wq);
+        Fc[(size_t)i * (irc_tc::KP / 8) + j] = *reinterpret_cast<uint4 *>(wc);
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    }
+    return fn;
+}
+
+// Tensor map over a [rows x 64] BF16 matrix, 128-row boxes, 128-byte swizzle.
+int make_map(CUtensorMap *m, void *base, int rows)
+{
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) { irc_host::set_error("cuTensorMapEncodeTiled unavailable"); return IRC_E_CUDA; }
+    cuuint64_t dims[2] = {(cuuint64_t)irc_tc::KP, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)irc_tc::KP * 2};
+    cuuint32_t box[2] = {(cuuint32_t)irc_tc::KP, (cuuint32_t)irc_tc::BN};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { irc_host::set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return IRC_E_CUDA; }
+    return IRC_OK;
+}
+
+}  // namespace
+
+// Plan-owned tensor-core operand buffers (irc_site.cu) and the exact
+// fallback for queries whose candidate list overflowed (irc_exact.cu).
+int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, size_t row_bytes);
+int irc_exact_overflow_drain(irc_plan *pl, const float *F, int nC, int knn, float *vrKnn, float *rho,
+                             int32_t *miKnn, float *d2Knn, cudaStream_t s);
+
+int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, float *vrKnn, float *rho,
+                    int32_t *miKnn, float *d2Knn, cudaStream_t s)
+{
+    if (mode != IRC_MODE_BF16) {
+        irc_host::set_error("irc_site_knn: FP8 tensor-core mode not available");
+        return IRC_E_UNSUPPORTED;
+    }
+    if (nC + 6 > irc_tc::KP) { irc_host::set_error("irc_site_knn(BF16): nC=%d > %d", nC, irc_tc::KP - 6); return IRC_E_NC; }
+    if (knn > irc_tc::KNN_MAX) { irc_host::set_error("irc_site_knn(BF16): knn %d > %d", knn, irc_tc::KNN_MAX); return IRC_E_INVAL; }
+    const int nF = pl->dev.nF;
+    void *fq, *fc;
+    int rc = irc_plan_tc_buffers(pl, &fq, &fc, irc_tc::KP * 2);
+    if (rc != IRC_OK) return rc;
+    cudaError_t e = cudaMemsetAsync(pl->scratch, 0, sizeof(int), s);       // overflow-queue count
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(BF16): memset");
+    k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, (uint4 *)fq, (uint4 *)fc);
+    IRC_CHECK_LAUNCH("irc_site_knn(BF16) prep");
+    CUtensorMap mq, mc;
+    if ((rc = make_map(&mq, fq, nF)) != IRC_OK) return rc;
+    if ((rc = make_map(&mc, fc, nF)) != IRC_OK) return rc;
+    rc = irc_tc::launch_knn_bf16(mq, mc, pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
+    if (rc != IRC_OK) return rc;
+    return irc_exact_overflow_drain(pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
+}
