@@ -262,6 +262,8 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     pl->dev.rn = base + off_rn;
     for (int k = 0; k < irc::kNumTileSizes; ++k) pl->dev.tile_off[k] = base + off_tile[k];
     pl->scratch = (int32_t *)pl->dmem + img.size();
+    e = cudaMemset(pl->scratch, 0, irc::kScratchLists * sizeof(int32_t));      // counters and error word
+    if (e != cudaSuccess) { cudaFree(pl->dmem); free(pl); return irc_host::cuda_status(e, "irc_plan_create: clear"); }
     pl->dev.nChunks = nChunks;
     pl->dev.q_base = q_base;
     pl->dev.n_out = n_out;
