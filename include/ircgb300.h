@@ -139,6 +139,29 @@ int irc_site_delta(irc_plan *plan, const float *F, int nC, const float *R, int n
                    int mode, int knn, const int32_t *miKnn, const float *d2Knn,
                    float *delta, int32_t *nneigh, void *stream);
 
+/* irc_site_knn in IRC_MODE_EXACT for callers that cannot allocate device
+ * memory -- hosts whose device memory is reserved up front by their own pool
+ * (a MATLAB gpuArray workspace, a real-time acquisition loop that must not
+ * hit the device-wide synchronisation of cudaMalloc/cudaFree), or code
+ * running where allocation is not allowed.  No counterpart in the reference.
+ * It takes the plan arrays as HOST pointers (same meaning as
+ * irc_plan_create) plus the inputs and outputs of irc_site_knn, and calls no
+ * cudaMalloc/cudaFree or other allocating routine: the device copy of the
+ * plan, its tile table and the overflow queue live in one fixed 8 MiB array
+ * inside the library, held by every GPU that loads it until the process
+ * exits.  The plan must fit that array: 4 + 2*n_out + 3*nChunks + 2 +
+ * 2*nRuns int32 words <= 2^21 (about a million queries); larger plans are
+ * rejected with IRC_E_INVAL and a message.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Every call
+ * shares the array and overwrites it, so calls that overlap on the GPU (two
+ * streams, two host threads) race: serialise them on one stream.  Outputs
+ * equal those of irc_site_knn(IRC_MODE_EXACT) bit for bit. */
+int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t *q0, const int32_t *nq,
+                               const int32_t *roff, const int32_t *rs, const int32_t *rn, int nChunks,
+                               int q_base, int n_out, int nF, int knn, float *vrKnn, float *rho,
+                               int32_t *miKnn, float *d2Knn, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

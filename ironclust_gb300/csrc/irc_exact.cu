@@ -19,6 +19,7 @@
 // spike would rank earlier in the list).  Queries without one -- local
 // density peaks -- go to a drift-window scan over all linked candidates.
 #include <cstdio>
+#include <mutex>
 
 #include "irc_common.cuh"
 #include "irc_plan.cuh"
@@ -384,5 +385,138 @@ int irc_exact_overflow_drain(irc_plan *pl, const float *F, int nC, int knn, floa
     irc_plan_scratch(pl, &cnt, &la, &lb);
     k_exact_overflow<<<kQueueBlocks, 256, 0, s>>>(pl->dev, F, nC, knn, cnt, la, vrKnn, rho, miKnn, d2Knn);
     IRC_CHECK_LAUNCH("irc_site_knn overflow drain");
+    return IRC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the EXACT site kNN (irc_site_knn_exact_noalloc).
+//
+// For callers that cannot call cudaMalloc: everything the kernels need
+// besides the caller's inputs and outputs -- the device copy of the plan,
+// the tile table, the overflow queue and its counter -- lives in the fixed
+// array below, which every GPU that loads the library holds until the
+// process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocWords = (size_t)2 << 20;     // 8 MiB of int32 words
+static __device__ __align__(256) int32_t g_noalloc_scratch[kNoAllocWords];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// with that device current (a host-side reference to the array is only a
+// stand-in, not a device address).
+constexpr int kMaxDevices = 64;
+int32_t *g_noalloc_ptr[kMaxDevices];
+std::mutex g_noalloc_mu;
+
+int noalloc_scratch(int32_t **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn_exact_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) {
+        irc_host::set_error("irc_site_knn_exact_noalloc: device %d out of range", dev);
+        return IRC_E_INVAL;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn_exact_noalloc: cudaGetSymbolAddress");
+        g_noalloc_ptr[dev] = (int32_t *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return IRC_OK;
+}
+
+// tile_off[i] = sum_{j<i} ceil(nq[j] / QB), one block, chunked scan.
+__global__ void k_noalloc_tiles(const int32_t *__restrict__ nq, int nChunks, int qb, int32_t *__restrict__ tile_off)
+{
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int per = (nChunks + nt - 1) / nt;
+    const int lo = min(t * per, nChunks), hi = min(lo + per, nChunks);
+    int32_t s = 0;
+    for (int i = lo; i < hi; ++i) s += (nq[i] + qb - 1) / qb;
+    part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        int32_t acc = 0;
+        for (int i = 0; i < nt; ++i) { const int32_t v = part[i]; part[i] = acc; acc += v; }
+    }
+    __syncthreads();
+    int32_t acc = part[t];
+    for (int i = lo; i < hi; ++i) { tile_off[i] = acc; acc += (nq[i] + qb - 1) / qb; }
+    if (hi == nChunks && lo < hi) tile_off[nChunks] = acc;
+    if (nChunks == 0 && t == 0) tile_off[0] = 0;
+}
+
+}  // namespace
+
+extern "C" int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t *q0, const int32_t *nq,
+                                          const int32_t *roff, const int32_t *rs, const int32_t *rn, int nChunks,
+                                          int q_base, int n_out, int nF, int knn, float *vrKnn, float *rho,
+                                          int32_t *miKnn, float *d2Knn, void *stream)
+{
+    const char *me = "irc_site_knn_exact_noalloc";
+    if (!F || !q0 || !nq || !roff || !rs || !rn || !vrKnn || !miKnn || nChunks <= 0 || n_out <= 0 || nF <= 0) {
+        irc_host::set_error("%s: null pointer or empty plan", me);
+        return IRC_E_INVAL;
+    }
+    if (nC > IRC_NC_MAX) { irc_host::set_error("%s: nC=%d > %d", me, nC, IRC_NC_MAX); return IRC_E_NC; }
+    if (nC <= 0 || knn <= 0 || knn > kCap / 2) { irc_host::set_error("%s: bad nC=%d / knn=%d", me, nC, knn); return IRC_E_INVAL; }
+    const int nRuns = roff[nChunks];
+    const size_t need = (size_t)irc::kScratchLists + 2 * (size_t)n_out + 3 * (size_t)nChunks + 2 + 2 * (size_t)(nRuns > 0 ? nRuns : 0);
+    if (roff[0] != 0 || nRuns <= 0 || need > kNoAllocWords) {
+        irc_host::set_error("%s: plan needs %zu scratch words, the fixed array holds %zu "
+                            "(n_out + 1.5*chunks + runs must stay below ~1M)", me, need, kNoAllocWords);
+        return IRC_E_INVAL;
+    }
+    int tiles = 0;
+    for (int i = 0; i < nChunks; ++i) {
+        if (nq[i] <= 0 || q0[i] < q_base || q0[i] + nq[i] > q_base + n_out || q0[i] + nq[i] > nF ||
+            roff[i + 1] <= roff[i]) {
+            irc_host::set_error("%s: chunk %d out of range", me, i);
+            return IRC_E_INVAL;
+        }
+        for (int r = roff[i]; r < roff[i + 1]; ++r)
+            if (rs[r] < 0 || rn[r] <= 0 || (long long)rs[r] + rn[r] > nF) {
+                irc_host::set_error("%s: run %d out of range", me, r);
+                return IRC_E_INVAL;
+            }
+        tiles += (nq[i] + kQB - 1) / kQB;
+    }
+    int32_t *base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc != IRC_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    // layout: scratch words | 2 queues of n_out | q0 | nq | roff | rs | rn | tile table
+    int32_t *d_q0 = base + irc::kScratchLists + 2 * (size_t)n_out;
+    int32_t *d_nq = d_q0 + nChunks;
+    int32_t *d_roff = d_nq + nChunks;
+    int32_t *d_rs = d_roff + nChunks + 1;
+    int32_t *d_rn = d_rs + nRuns;
+    int32_t *d_tile = d_rn + nRuns;
+    cudaError_t e = cudaMemsetAsync(base, 0, irc::kScratchLists * sizeof(int32_t), s);    // counters start at zero
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_q0, q0, 4 * (size_t)nChunks, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_nq, nq, 4 * (size_t)nChunks, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_roff, roff, 4 * ((size_t)nChunks + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rs, rs, 4 * (size_t)nRuns, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rn, rn, 4 * (size_t)nRuns, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn_exact_noalloc: upload");
+    k_noalloc_tiles<<<1, 1024, 0, s>>>(d_nq, nChunks, kQB, d_tile);
+    IRC_CHECK_LAUNCH("irc_site_knn_exact_noalloc tiles");
+    irc::PlanDev p;
+    p.q0 = d_q0; p.nq = d_nq; p.roff = d_roff; p.rs = d_rs; p.rn = d_rn;
+    for (int k = 0; k < irc::kNumTileSizes; ++k) p.tile_off[k] = d_tile;     // only the 16-query table is read
+    p.nChunks = nChunks; p.q_base = q_base; p.n_out = n_out; p.nF = nF; p.nRuns = nRuns;
+    const size_t smem = (size_t)kQB * kCap * 8 + (size_t)kQB * kThreads * 4;
+    e = cudaFuncSetAttribute(k_site_knn_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn_exact_noalloc: smem attribute");
+    int32_t *cnt = base, *queue = base + irc::kScratchLists;
+    k_site_knn_exact<<<tiles, kThreads, smem, s>>>(p, F, nC, knn, vrKnn, rho, miKnn, d2Knn, cnt, queue);
+    IRC_CHECK_LAUNCH("irc_site_knn_exact_noalloc");
+    k_exact_overflow<<<kQueueBlocks, 256, 0, s>>>(p, F, nC, knn, cnt, queue, vrKnn, rho, miKnn, d2Knn);
+    IRC_CHECK_LAUNCH("irc_site_knn_exact_noalloc overflow");
     return IRC_OK;
 }
