@@ -212,52 +212,61 @@ k_site_knn_exact(irc::PlanDev p, const float *__restrict__ F, int nC, int knn,
     }
 }
 
-// Warp per overflowing query: k ordered scans, each the smallest key above
-// the previous one.
-__global__ void k_exact_overflow(irc::PlanDev p, const float *__restrict__ F, int nC, int knn,
-                                 const int *__restrict__ ovf_count, const int *__restrict__ ovf_list,
-                                 float *__restrict__ vrKnn, float *__restrict__ rho,
-                                 int *__restrict__ miKnn, float *__restrict__ d2Knn)
+// One CTA per queued query: k ordered scans of all linked candidates, each a
+// block-wide minimum of the keys above the previous one.  Serves the rare
+// queries whose candidate list overflowed (mass ties, or an unlucky spread of
+// the tensor-core filter's list parts).
+__global__ void __launch_bounds__(kThreads)
+k_exact_overflow(irc::PlanDev p, const float *__restrict__ F, int nC, int knn,
+                 const int *__restrict__ ovf_count, const int *__restrict__ ovf_list,
+                 float *__restrict__ vrKnn, float *__restrict__ rho,
+                 int *__restrict__ miKnn, float *__restrict__ d2Knn)
 {
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < *ovf_count; w += nwarps) {
-    const int q = ovf_list[w];
-    int lo = 0, hi = p.nChunks;
-    while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (__ldg(p.q0 + mid) <= q) lo = mid; else hi = mid; }
-    const int r0 = __ldg(p.roff + lo), r1 = __ldg(p.roff + lo + 1);
-    const float *a = F + (size_t)q * nC;
-    const size_t o = (size_t)(q - p.q_base);
-    unsigned long long prev = 0;
-    bool have_prev = false;
-    for (int k = 0; k < knn; ++k) {
-        unsigned long long best = ~0ull;
-        for (int r = r0; r < r1; ++r) {
-            const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
-            for (int i = lane; i < rn; i += 32) {
-                const float *b = F + (size_t)(rs + i) * nC;
+    __shared__ unsigned long long red[kThreads / 32];
+    __shared__ unsigned long long sBest;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = *ovf_count;
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+        const int q = ovf_list[w];
+        int lo = 0, hi = p.nChunks;
+        while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (__ldg(p.q0 + mid) <= q) lo = mid; else hi = mid; }
+        const int r0 = __ldg(p.roff + lo), r1 = __ldg(p.roff + lo + 1);
+        const float *a = F + (size_t)q * nC;
+        const size_t o = (size_t)(q - p.q_base);
+        unsigned long long prev = 0;
+        bool have_prev = false;
+        for (int k = 0; k < knn; ++k) {
+            unsigned long long best = ~0ull;
+            walk_stripe(p, r0, r1, threadIdx.x, [&](int iB) {
+                const float *b = F + (size_t)iB * nC;
                 float acc = 0.0f;
                 for (int c = 0; c < nC; ++c) acc = irc::dterm(acc, __ldg(b + c), __ldg(a + c));
-                if (!(acc > 0.0f)) continue;
-                const unsigned long long key = dkey(acc, rs + i);
+                if (!(acc > 0.0f) || !(acc < kInfSentinel)) return;
+                const unsigned long long key = dkey(acc, iB);
                 if ((!have_prev || key > prev) && key < best) best = key;
+            });
+            best = irc::warp_min_u64(best);
+            if (lane == 0) red[warp] = best;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned long long b = red[0];
+                for (int i = 1; i < kThreads / 32; ++i) b = red[i] < b ? red[i] : b;
+                sBest = b;
+                const bool ok = b != ~0ull;
+                const float d2 = ok ? __uint_as_float((unsigned)(b >> 32)) : kInfSentinel;
+                const int idx = ok ? (int)(b & 0xffffffffu) : q;
+                miKnn[(size_t)k + (size_t)knn * o] = idx + 1;
+                if (d2Knn) d2Knn[(size_t)k + (size_t)knn * o] = d2;
+                if (k == knn - 1) {
+                    const float v = irc::ref_sqrt_abs(d2);
+                    vrKnn[o] = v;
+                    if (rho) rho[o] = __fdiv_rn(1.0f, v);
+                }
             }
+            __syncthreads();
+            best = sBest;
+            if (best != ~0ull) { prev = best; have_prev = true; }
         }
-        best = irc::warp_min_u64(best);
-        const bool ok = best != ~0ull;
-        const float d2 = ok ? __uint_as_float((unsigned)(best >> 32)) : kInfSentinel;
-        const int idx = ok ? (int)(best & 0xffffffffu) : q;
-        if (lane == 0) {
-            miKnn[(size_t)k + (size_t)knn * o] = idx + 1;
-            if (d2Knn) d2Knn[(size_t)k + (size_t)knn * o] = d2;
-            if (k == knn - 1) {
-                const float v = irc::ref_sqrt_abs(d2);
-                vrKnn[o] = v;
-                if (rho) rho[o] = __fdiv_rn(1.0f, v);
-            }
-        }
-        if (ok) { prev = best; have_prev = true; }
-    }
     }
 }
 
@@ -265,7 +274,7 @@ __global__ void k_exact_overflow(irc::PlanDev p, const float *__restrict__ F, in
 __global__ void k_delta_list(irc::PlanDev p, const float *__restrict__ R, int knn,
                              const int *__restrict__ miKnn, const float *__restrict__ d2Knn,
                              float *__restrict__ delta, int *__restrict__ nneigh,
-                             int *__restrict__ fb_count, int *__restrict__ fb_list)
+                             int *__restrict__ fb_flag)
 {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= p.n_out) return;
@@ -273,6 +282,7 @@ __global__ void k_delta_list(irc::PlanDev p, const float *__restrict__ R, int kn
     const float rq = __ldg(R + q);
     const int *mi = miKnn + (size_t)knn * o;
     const float *dk = d2Knn + (size_t)knn * o;
+    int miss = 1;
     for (int k = 0; k < knn; ++k) {
         const float d2 = __ldg(dk + k);
         if (!(d2 < kInfSentinel)) break;                 // list exhausted
@@ -280,48 +290,117 @@ __global__ void k_delta_list(irc::PlanDev p, const float *__restrict__ R, int kn
         if (!(__ldg(R + j) <= rq)) {                     // reference mask: rb <= ra is excluded
             delta[o] = __fmul_rn(irc::ref_sqrt_abs(d2), rq);
             nneigh[o] = j + 1;
-            return;
+            miss = 0;
+            break;
         }
     }
-    const int i = atomicAdd(fb_count, 1);
-    fb_list[i] = q;
+    fb_flag[o] = miss;
 }
 
-// Drift-window fallback: warp per queued query, all linked candidates.
-__global__ void k_delta_scan(irc::PlanDev p, const float *__restrict__ F, const float *__restrict__ R,
-                             int nC, const int *__restrict__ fb_count, const int *__restrict__ fb_list,
-                             float *__restrict__ delta, int *__restrict__ nneigh)
+// One CTA per chunk: compact the chunk's flagged queries (in order) into the
+// chunk's own segment of fb_list, then claim one (chunk, 16-query tile) item
+// per started 16 of them.  item = {chunk, (first << 5) | count}.
+__global__ void __launch_bounds__(kThreads)
+k_delta_compact(irc::PlanDev p, const int *__restrict__ fb_flag, int *__restrict__ fb_list,
+                int *__restrict__ n_items, int2 *__restrict__ items)
 {
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < *fb_count; w += nwarps) {
-    const int q = fb_list[w];
-    int lo = 0, hi = p.nChunks;
-    while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (__ldg(p.q0 + mid) <= q) lo = mid; else hi = mid; }
-    const int r0 = __ldg(p.roff + lo), r1 = __ldg(p.roff + lo + 1);
-    const float *a = F + (size_t)q * nC;
-    const float rq = __ldg(R + q);
-    unsigned long long best = ~0ull;
-    for (int r = r0; r < r1; ++r) {
-        const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
-        for (int i = lane; i < rn; i += 32) {
-            if (__ldg(R + rs + i) <= rq) continue;
-            const float *b = F + (size_t)(rs + i) * nC;
-            float acc = 0.0f;
-            for (int c = 0; c < nC; ++c) acc = irc::dterm(acc, __ldg(b + c), __ldg(a + c));
-            if (!(acc > 0.0f) || !(acc < kInfSentinel)) continue;
-            const unsigned long long key = dkey(acc, rs + i);
-            best = key < best ? key : best;
+    __shared__ int wsum[kThreads / 32];
+    __shared__ int running, base;
+    const int chunk = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int q0 = __ldg(p.q0 + chunk), nq = __ldg(p.nq + chunk), seg = q0 - p.q_base;
+    if (threadIdx.x == 0) running = 0;
+    __syncthreads();
+    for (int start = 0; start < nq; start += kThreads) {
+        const int i = start + threadIdx.x;
+        const int f = i < nq ? fb_flag[seg + i] : 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        int off = running;
+        for (int w = 0; w < warp; ++w) off += wsum[w];
+        if (f) fb_list[seg + off + __popc(bal & ((1u << lane) - 1u))] = q0 + i;
+        __syncthreads();
+        if (threadIdx.x == 0) for (int w = 0; w < kThreads / 32; ++w) running += wsum[w];
+        __syncthreads();
+    }
+    const int total = running, ntile = (total + kQB - 1) / kQB;
+    if (threadIdx.x == 0) base = ntile ? atomicAdd(n_items, ntile) : 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < ntile; j += kThreads)
+        items[base + j] = make_int2(chunk, ((j * kQB) << 5) | min(kQB, total - j * kQB));
+}
+
+// Drift-window fallback, 16 queued queries of one chunk per CTA: every
+// linked candidate is loaded once for the 16 and kept per query when its rho
+// exceeds the query's (the search_delta_drift mask), ties by (d2, index).
+__global__ void __launch_bounds__(kThreads)
+k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restrict__ R, int nC,
+              const int *__restrict__ n_items, const int2 *__restrict__ items, const int *__restrict__ fb_list,
+              float *__restrict__ delta, int *__restrict__ nneigh)
+{
+    __shared__ __align__(16) float sA[IRC_NC_MAX * kQB];
+    __shared__ float sRA[kQB];
+    __shared__ int sQ[kQB];
+    __shared__ unsigned long long red[kQB][kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int total = *n_items;
+    for (int it = blockIdx.x; it < total; it += gridDim.x) {
+        const int2 item = items[it];
+        const int chunk = item.x, first = item.y >> 5, n = item.y & 31;
+        const int seg = __ldg(p.q0 + chunk) - p.q_base;
+        if (threadIdx.x < kQB) {
+            const int q = fb_list[seg + first + min((int)threadIdx.x, n - 1)];
+            sQ[threadIdx.x] = q;
+            sRA[threadIdx.x] = __ldg(R + q);
         }
-    }
-    best = irc::warp_min_u64(best);
-    if (lane == 0) {
-        const size_t o = (size_t)(q - p.q_base);
-        const bool ok = best != ~0ull;
-        const float d2 = ok ? __uint_as_float((unsigned)(best >> 32)) : kInfSentinel;
-        delta[o] = __fmul_rn(irc::ref_sqrt_abs(d2), rq);
-        nneigh[o] = (ok ? (int)(best & 0xffffffffu) : q) + 1;
-    }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nC * kQB; i += kThreads) {
+            const int c = i / kQB, q = i - c * kQB;
+            sA[i] = __ldg(F + (size_t)sQ[q] * nC + c);
+        }
+        __syncthreads();
+        unsigned long long best[kQB];
+#pragma unroll
+        for (int q = 0; q < kQB; ++q) best[q] = ~0ull;
+        const int r0 = __ldg(p.roff + chunk), r1 = __ldg(p.roff + chunk + 1);
+        for (int r = r0; r < r1; ++r) {
+            const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
+            for (int i = threadIdx.x; i < rn; i += kThreads) {
+                const int iB = rs + i;
+                const float rb = __ldg(R + iB);
+                unsigned live = 0;
+#pragma unroll
+                for (int q = 0; q < kQB; ++q)
+                    if (!(rb <= sRA[q])) live |= 1u << q;
+                if (!live) continue;
+                float acc[kQB];
+                dist_qb<kQB>(F + (size_t)iB * nC, nC, sA, acc);
+#pragma unroll
+                for (int q = 0; q < kQB; ++q)
+                    if (((live >> q) & 1u) && acc[q] > 0.0f && acc[q] < kInfSentinel) {
+                        const unsigned long long key = dkey(acc[q], iB);
+                        best[q] = key < best[q] ? key : best[q];
+                    }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kQB; ++q) {
+            const unsigned long long b = irc::warp_min_u64(best[q]);
+            if (lane == 0) red[q][warp] = b;
+        }
+        __syncthreads();
+        if (threadIdx.x < n) {
+            const int q = threadIdx.x;
+            unsigned long long b = red[q][0];
+            for (int w = 1; w < kThreads / 32; ++w) b = red[q][w] < b ? red[q][w] : b;
+            const int qq = sQ[q];
+            const size_t o = (size_t)(qq - p.q_base);
+            const bool ok = b != ~0ull;
+            const float d2 = ok ? __uint_as_float((unsigned)(b >> 32)) : kInfSentinel;
+            delta[o] = __fmul_rn(irc::ref_sqrt_abs(d2), sRA[q]);
+            nneigh[o] = (ok ? (int)(b & 0xffffffffu) : qq) + 1;
+        }
+        __syncthreads();
     }
 }
 
@@ -365,14 +444,18 @@ int irc_site_delta_list(irc_plan *pl, const float *F, int nC, const float *R, in
     int *cnt, *la, *lb;
     int rc = irc_plan_scratch(pl, &cnt, &la, &lb);
     if (rc != IRC_OK) return rc;
-    cudaError_t e = cudaMemsetAsync(cnt + 1, 0, sizeof(int), s);
+    // flags in list a, compacted queries in list b, (chunk, tile) items after them
+    int *n_items = cnt + irc::kScratchItems;
+    int2 *items = reinterpret_cast<int2 *>(lb + pl->dev.n_out);
+    cudaError_t e = cudaMemsetAsync(n_items, 0, sizeof(int), s);
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_delta: memset");
     const int n = pl->dev.n_out;
-    k_delta_list<<<(n + 255) / 256, 256, 0, s>>>(pl->dev, R, knn, miKnn, d2Knn, delta, nneigh, cnt + 1, lb);
+    k_delta_list<<<(n + 255) / 256, 256, 0, s>>>(pl->dev, R, knn, miKnn, d2Knn, delta, nneigh, la);
     IRC_CHECK_LAUNCH("irc_site_delta list");
-    k_delta_scan<<<kQueueBlocks, 256, 0, s>>>(pl->dev, F, R, nC, cnt + 1, lb,
-                                                                              delta, nneigh);
-    IRC_CHECK_LAUNCH("irc_site_delta scan");
+    k_delta_compact<<<pl->dev.nChunks, kThreads, 0, s>>>(pl->dev, la, lb, n_items, items);
+    IRC_CHECK_LAUNCH("irc_site_delta compact");
+    k_delta_tiles<<<kQueueBlocks, kThreads, 0, s>>>(pl->dev, F, R, nC, n_items, items, lb, delta, nneigh);
+    IRC_CHECK_LAUNCH("irc_site_delta tiles");
     return IRC_OK;
 }
 

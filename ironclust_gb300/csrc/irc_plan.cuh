@@ -8,6 +8,7 @@ namespace irc {
 // [2] device error word (a bounded wait gave up), [3] unused; the two query
 // lists of n_out entries follow.
 constexpr int kScratchErr = 2;
+constexpr int kScratchItems = 3;      // count of delta-fallback (chunk, tile) items
 constexpr int kScratchLists = 4;
 
 // Query-tile sizes for which a plan precomputes its tile tables.

@@ -245,7 +245,10 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
         pl->ntiles[k] = acc;
     }
     cudaGetDevice(&pl->device);
-    const size_t scratch_ints = irc::kScratchLists + 2 * (size_t)n_out;
+    if (img.size() & 1) img.push_back(0);          // scratch starts 8-byte aligned (int2 items)
+    // 4 words, two query lists of n_out, and the (chunk, tile) items of the
+    // delta fallback: at most n_out/16 + nChunks pairs
+    const size_t scratch_ints = irc::kScratchLists + 2 * (size_t)n_out + 2 * ((size_t)n_out / 16 + nChunks + 1);
     cudaError_t e = cudaMalloc(&pl->dmem, (img.size() + scratch_ints) * sizeof(int32_t));
     if (e != cudaSuccess) {
         free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn); free(pl);

@@ -1,21 +1,24 @@
 // irc_tc.cu -- tensor-core (tcgen05) site kNN: BF16 distance filter, exact
 // FP32 re-rank, FP64 at the k-th-neighbour boundary.
 //
-// Per CTA: 128 queries of one drift chunk (TMEM lanes, one query per
-// epilogue thread) against every linked candidate, in 128-candidate tiles
-// (TMEM columns, two accumulator buffers).  The BF16 operand rows (see
-// irc_tc_host.cu) make every accumulator the approximate squared distance.
-// Warp roles: warp 0 issues TMA loads (4-stage ring), warp 1 owns TMEM and
-// issues tcgen05.mma from one thread, warps 2-5 (one per TMEM lane quarter)
-// are the epilogue.  The candidate tiles are streamed twice:
-//   pass 1  every thread folds each tile into 128 per-column minima (one
-//           FMNMX per pair, no branches); the 64th smallest of those minima
-//           is an upper bound tau on the 64th nearest approximate distance
-//           (64 distinct candidates lie at or below it);
-//   pass 2  candidates with approximate distance <= tau are appended, with
-//           predicated stores, to the query's shared-memory list (~90
-//           entries on random data; capacity 224, overflow goes to an exact
-//           fallback kernel).
+// Per CTA: 128 queries of one drift chunk (TMEM lanes) against every linked
+// candidate, in 128-candidate tiles (TMEM columns, two accumulator
+// buffers).  The BF16 operand rows (see irc_tc_host.cu) make every
+// accumulator the approximate squared distance.  Warp roles: warp 0 issues
+// TMA loads (4-stage ring), warp 1 owns TMEM and issues tcgen05.mma from one
+// thread, warps 2-9 are the epilogue: two warps per TMEM lane quarter, each
+// owning one half (64 columns) of every tile, so a query is served by two
+// threads.  The candidate tiles are streamed twice:
+//   pass 1  every thread folds its half-tiles into 64 per-column minima (one
+//           FMNMX per pair, no branches); per query, the 64th smallest of the
+//           128 minima of both halves is an upper bound tau on the 64th
+//           nearest approximate distance (64 distinct candidates lie at or
+//           below it);
+//   pass 2  every thread marks the pairs at or below tau in a 32-bit mask
+//           (one compare and one predicated OR per pair) and appends only the
+//           marked candidates to its half-list in shared memory (~90 per
+//           query on random data; 96 per half; an overflowing query is
+//           finished by the exact fallback kernel).
 // Every listed candidate is then re-ranked with the reference FP32
 // arithmetic (exact), zero distances dropped, sorted by (distance, index)
 // with a warp bitonic network; candidates within 16 ulps of the k-th
@@ -35,17 +38,21 @@ using irc_tc::BM;
 using irc_tc::BN;
 using irc_tc::KP;
 constexpr int STAGES = 4;
-constexpr int CAP = 224;                          // list capacity per query
-constexpr int LROW = CAP + 32 + 1;                // list row (u32): CAP + one chunk of slack + pad
+constexpr int PARTS = 4;                          // epilogue warps per TMEM lane quarter
+constexpr int PART = BN / PARTS;                  // columns of a tile per epilogue warp (32)
+constexpr int CAPP = 64;                          // list capacity per query and part
+constexpr int LROWP = CAPP + 1;                   // part-list row (u32), padded
 constexpr int BROW = BN + 1;                      // per-column minima row (f32) during the threshold step
-constexpr int EPI_WARPS = 4;
+constexpr int EPI_WARPS = 4 * PARTS;
+constexpr int EPI_THREADS = 32 * EPI_WARPS;
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TILE_BYTES = BN * KP * 2;      // 16 KB (A tile has the same size)
 constexpr uint32_t TMEM_COLS = 2 * BN;
-constexpr size_t LIST_BYTES = (size_t)LROW * BM * 4;
-constexpr size_t WARP_KEYS = 256;                 // re-rank keys per epilogue warp
-constexpr size_t SMEM_BYTES =
-    1024 /*align slack*/ + TILE_BYTES * (1 + STAGES) + LIST_BYTES + EPI_WARPS * WARP_KEYS * 8 + 256;
+constexpr size_t LIST_BYTES = (size_t)LROWP * PARTS * BM * 4;
+constexpr int WARP_KEYS = 64;                     // sorted re-rank keys kept per epilogue warp
+constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + TILE_BYTES * (1 + STAGES) + LIST_BYTES +
+                              EPI_WARPS * WARP_KEYS * 8 + BM * 4 /*tau*/ + PARTS * BM * 4 /*counts*/ + 256;
+static_assert(PART == 32, "one TMEM load of 32 columns per warp and tile");
 static_assert((size_t)BROW * BM * 4 <= LIST_BYTES, "minima rows alias the list area");
 static_assert(SMEM_BYTES <= 232448, "shared memory budget");
 
@@ -110,20 +117,29 @@ __device__ __forceinline__ void emit(int e, unsigned long long key, int q, int k
     }
 }
 
-// Exact re-rank of the cL listed candidates of query q (warp-cooperative).
+// Exact re-rank of the candidates listed for query q in its PARTS part-lists
+// (lists[p*LROWP + i], i < cnt[p]), warp-cooperative.  Requires knn <= 32.
 template <int PER>
-__device__ __forceinline__ void rerank(const uint32_t *__restrict__ lrow, int cL, int q, const float *__restrict__ F,
-                                       int nC, int knn, size_t o, unsigned long long *ws, int lane, int *miKnn,
-                                       float *d2Knn, float *vrKnn, float *rho)
+__device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const int (&cnt)[PARTS], int q,
+                                       const float *__restrict__ F, int nC, int knn, size_t o,
+                                       unsigned long long *ws, int lane, int *miKnn, float *d2Knn, float *vrKnn,
+                                       float *rho)
 {
     const float *a = F + (size_t)q * nC;
+    int cL = 0;
+#pragma unroll
+    for (int p = 0; p < PARTS; ++p) cL += cnt[p];
     unsigned long long kv[PER];
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = i * 32 + lane;
         kv[i] = ~0ull;
         if (e < cL) {
-            const int idx = (int)lrow[e];
+            int p = 0, r = e;
+#pragma unroll
+            for (int u = 0; u < PARTS - 1; ++u)
+                if (p == u && r >= cnt[u]) { r -= cnt[u]; p = u + 1; }
+            const int idx = (int)lists[p * LROWP + r];
             const float *bb = F + (size_t)idx * nC;
             float acc = 0.0f;
             for (int c = 0; c < nC; ++c) acc = irc::dterm(acc, __ldg(bb + c), __ldg(a + c));
@@ -133,7 +149,8 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lrow, int cL
     }
     warp_bitonic<unsigned long long, PER>(kv, lane);
 #pragma unroll
-    for (int i = 0; i < PER; ++i) ws[lane * PER + i] = kv[i];
+    for (int i = 0; i < PER; ++i)
+        if (lane * PER + i < WARP_KEYS) ws[lane * PER + i] = kv[i];
     __syncwarp();
     // boundary band: keys within 16 ulps of the k-th distance, ordered by FP64
     const unsigned long long kk = ws[knn - 1];
@@ -145,7 +162,7 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lrow, int cL
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const int e = lane * PER + i;
-            if (kv[i] != ~0ull && fabsf(__uint_as_float((unsigned)(kv[i] >> 32)) - vk) <= tol) {
+            if (e < WARP_KEYS && kv[i] != ~0ull && fabsf(__uint_as_float((unsigned)(kv[i] >> 32)) - vk) <= tol) {
                 mlo = min(mlo, (unsigned)e);
                 mhi = max(mhi, (unsigned)e + 1u);
             }
@@ -173,9 +190,7 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lrow, int cL
     __syncwarp();
 }
 
-}  // namespace
-
-namespace {
+__device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory"); }
 
 __global__ void __launch_bounds__(THREADS, 1)
 k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
@@ -186,9 +201,11 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *sA = base;
     uint8_t *sB = base + TILE_BYTES;
-    uint32_t *lists = reinterpret_cast<uint32_t *>(sB + STAGES * TILE_BYTES);          // [BM][LROW]
-    unsigned long long *wkeys = reinterpret_cast<unsigned long long *>(lists + (size_t)LROW * BM);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(wkeys + EPI_WARPS * WARP_KEYS);
+    uint32_t *lists = reinterpret_cast<uint32_t *>(sB + STAGES * TILE_BYTES);        // [BM][PARTS][LROWP]
+    unsigned long long *wkeys = reinterpret_cast<unsigned long long *>(lists + (size_t)LROWP * PARTS * BM);
+    float *sTau = reinterpret_cast<float *>(wkeys + EPI_WARPS * WARP_KEYS);          // [BM]
+    int *sCnt = reinterpret_cast<int *>(sTau + BM);                                  // [BM][PARTS], -1 = overflow
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sCnt + PARTS * BM);
     uint64_t *full = bars, *empty = bars + STAGES, *a_full = bars + 2 * STAGES;
     uint64_t *acc_full = a_full + 1, *acc_empty = a_full + 3, *mma_done = a_full + 5;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(a_full + 6);
@@ -265,37 +282,35 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue: one query per thread ----------------
-        const int quarter = warp & 3;
+        // ---------------- epilogue: one (query, 32-column part) per thread ----------------
+        const int ew = warp - 2;                      // 0..15
+        const int quarter = warp & 3;                 // TMEM lane quarter this warp may access
+        const int part = ew >> 2;                     // which 32 columns of every tile
         const int row = quarter * 32 + lane;
-        const uint32_t tlane = (uint32_t)(quarter * 32) << 16;
+        const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + part * PART;
         bool ok = true;
         int i = 0;
-        // pass 1: per-column minima
-        float bm[BN];
+        // pass 1: per-column minima of this part
+        float bm[PART];
 #pragma unroll
-        for (int c = 0; c < BN; ++c) bm[c] = __int_as_float(0x7f800000);
+        for (int c = 0; c < PART; ++c) bm[c] = __int_as_float(0x7f800000);
         for (int r = r0; r < r1 && ok; ++r) {
             const int rn = __ldg(p.rn + r);
             for (int t = 0; t < rn; t += BN, ++i) {
                 const int b = i & 1;
                 if (!(ok = sm100::mbar_wait(&acc_full[b], (i >> 1) & 1, abort_flag))) break;
                 sm100::tc_fence_after();
-                const int nvalid = min(BN, rn - t);
+                const int lim = min(BN, rn - t) - part * PART;    // valid columns in this part
+                if (lim > 0) {
+                    float v[32];
+                    sm100::tmem_ld32(tbase + b * BN, v);
+                    if (lim >= 32) {
 #pragma unroll
-                for (int g = 0; g < BN / 32; ++g) {
-                    if (g * 32 < nvalid) {
-                        float v[32];
-                        sm100::tmem_ld32(tmem + tlane + b * BN + g * 32, v);
-                        const int lim = nvalid - g * 32;
-                        if (lim >= 32) {
+                        for (int j = 0; j < 32; ++j) bm[j] = fminf(bm[j], v[j]);
+                    } else {
 #pragma unroll
-                            for (int j = 0; j < 32; ++j) bm[g * 32 + j] = fminf(bm[g * 32 + j], v[j]);
-                        } else {
-#pragma unroll
-                            for (int j = 0; j < 32; ++j)
-                                if (j < lim) bm[g * 32 + j] = fminf(bm[g * 32 + j], v[j]);
-                        }
+                        for (int j = 0; j < 32; ++j)
+                            if (j < lim) bm[j] = fminf(bm[j], v[j]);
                     }
                 }
                 sm100::tc_fence_before();
@@ -303,29 +318,27 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
                 if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
             }
         }
-        // threshold: 64th smallest column minimum of every query (warp sorts per row)
-        float tau;
+        // threshold: 64th smallest of the 128 column minima of every query
         {
-            float *brow = reinterpret_cast<float *>(lists) + (size_t)row * BROW;
+            float *brow = reinterpret_cast<float *>(lists) + (size_t)row * BROW + part * PART;
 #pragma unroll
-            for (int c = 0; c < BN; ++c) brow[c] = fmaxf(bm[c], 0.0f);
-            __syncwarp();
-            tau = __int_as_float(0x7f800000);
-            for (int L = 0; L < 32; ++L) {
-                const float *bl = reinterpret_cast<const float *>(lists) + (size_t)(quarter * 32 + L) * BROW;
+            for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
+            epi_barrier();
+            for (int L = 0; L < 32 / PARTS; ++L) {
+                const int rowL = quarter * 32 + part * (32 / PARTS) + L;
+                const float *bl = reinterpret_cast<const float *>(lists) + (size_t)rowL * BROW;
                 unsigned v4[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) v4[u] = __float_as_uint(bl[u * 32 + lane]);
                 warp_bitonic<unsigned, 4>(v4, lane);
                 const unsigned kth = __shfl_sync(0xffffffffu, v4[63 % 4], 63 / 4);
-                if (lane == L) tau = __uint_as_float(kth);
+                if (lane == 0) sTau[rowL] = __uint_as_float(kth);
             }
-            // the minima rows alias the list area: every epilogue warp is done
-            // reading them before any list is written
-            asm volatile("bar.sync 1, %0;" ::"n"(EPI_WARPS * 32) : "memory");
+            epi_barrier();              // minima rows are read; the list area may be reused
         }
-        // pass 2: collect candidates at or below tau
-        uint32_t *lrow = lists + (size_t)row * LROW;
+        const float tau = sTau[row];
+        // pass 2: collect the candidates at or below tau
+        uint32_t *lrow = lists + ((size_t)row * PARTS + part) * LROWP;
         int cnt = 0;
         bool ovf = false;
         for (int r = r0; r < r1 && ok; ++r) {
@@ -334,21 +347,21 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
                 const int b = i & 1;
                 if (!(ok = sm100::mbar_wait(&acc_full[b], (i >> 1) & 1, abort_flag))) break;
                 sm100::tc_fence_after();
-                const int nvalid = min(BN, rn - t);
+                const int lim = min(BN, rn - t) - part * PART;
+                if (lim > 0) {
+                    float v[32];
+                    sm100::tmem_ld32(tbase + b * BN, v);
+                    unsigned m = 0;
 #pragma unroll
-                for (int g = 0; g < BN / 32; ++g) {
-                    if (g * 32 < nvalid) {
-                        float v[32];
-                        sm100::tmem_ld32(tmem + tlane + b * BN + g * 32, v);
-                        const int lim = nvalid - g * 32;
-                        const uint32_t c0 = (uint32_t)(rs + t + g * 32);
-#pragma unroll
-                        for (int j = 0; j < 32; ++j)
-                            if (j < lim && v[j] <= tau) {
-                                lrow[cnt] = c0 + j;
-                                ++cnt;
-                            }
-                        if (cnt > CAP) { ovf = true; cnt = CAP; }
+                    for (int j = 0; j < 32; ++j)
+                        if (v[j] <= tau) m |= 1u << j;
+                    if (lim < 32) m &= (1u << lim) - 1u;
+                    if (cnt + __popc(m) > CAPP) { ovf = true; m = 0; }
+                    const uint32_t c0 = (uint32_t)(rs + t + part * PART);
+                    while (m) {
+                        const int j = __ffs(m) - 1;
+                        m &= m - 1u;
+                        lrow[cnt++] = c0 + (uint32_t)j;
                     }
                 }
                 sm100::tc_fence_before();
@@ -356,30 +369,35 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
                 if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
             }
         }
-        __syncwarp();
-        // exact re-rank, one query per warp step
-        unsigned long long *ws = wkeys + (size_t)(warp - 2) * WARP_KEYS;
-        for (int L = 0; L < 32 && ok; ++L) {
-            const int rowL = quarter * 32 + L;
+        sCnt[row * PARTS + part] = ovf ? -1 : cnt;
+        epi_barrier();
+        // exact re-rank: this warp serves 8 of its quarter's queries
+        unsigned long long *ws = wkeys + (size_t)ew * WARP_KEYS;
+        for (int L = 0; L < 32 / PARTS && ok; ++L) {
+            const int rowL = quarter * 32 + part * (32 / PARTS) + L;
             if (rowL >= nq) break;
             const int q = qs + rowL;
-            const int cL = __shfl_sync(0xffffffffu, cnt, L);
-            const bool oL = __shfl_sync(0xffffffffu, (int)ovf, L) != 0;
-            if (oL) {                                 // finished by the exact fallback kernel
+            int c[PARTS];
+            bool over = false, big = false;
+#pragma unroll
+            for (int u = 0; u < PARTS; ++u) { c[u] = sCnt[rowL * PARTS + u]; over |= c[u] < 0; }
+            if (over) {                               // finished by the exact fallback kernel
                 if (lane == 0) {
                     const int k = atomicAdd(scratch + 0, 1);
                     scratch[irc::kScratchLists + k] = q;
                 }
                 continue;
             }
-            const uint32_t *ll = lists + (size_t)rowL * LROW;
+            const int cL = c[0] + c[1] + c[2] + c[3];
+            big = cL > 128;
+            const uint32_t *lr = lists + (size_t)rowL * PARTS * LROWP;
             const size_t o = (size_t)(q - p.q_base);
             if (cL <= 64)
-                rerank<2>(ll, cL, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
-            else if (cL <= 128)
-                rerank<4>(ll, cL, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+                rerank<2>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+            else if (!big)
+                rerank<4>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
             else
-                rerank<8>(ll, cL, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+                rerank<8>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
         }
     }
     sm100::tc_fence_before();

@@ -57,6 +57,34 @@ def test_bf16_knn_matches_exact(gpu, case):
     assert rel.max() <= 1e-4, rel.max()
 
 
+def test_mass_ties_take_the_exact_fallback(gpu):
+    """400 identical spikes: every query near them sees hundreds of candidates
+    at one distance, so the candidate lists overflow and the exact fallback
+    kernel finishes those queries; results still equal the FP32 oracle."""
+    from ironclust_gb300.drift import build_plan
+    rng = np.random.default_rng(77)
+    F = rng.normal(0, 3, (3000, 24)).astype(np.float32)
+    F[1000:1400] = F[999]                                  # the blob
+    F[1400:1410] = F[999] + rng.normal(0, 0.01, (10, 24)).astype(np.float32)
+    vd = np.repeat(np.arange(3), 1000).astype(np.int32)
+    plan = build_plan(vd, np.ones(3000, bool), np.ones((3, 3), bool))
+    Fd = torch.from_numpy(F).to(gpu)
+    P = irc.Plan(plan)
+    idx, d2 = O.exact_knn_f32(F, plan, 30)
+    for mode in ("exact", "bf16"):
+        out = irc.site_knn(P, Fd, knn=30, mode=mode)
+        _lib.check(_lib.lib().irc_plan_check(P.h, irc._stream()), "irc_plan_check")
+        got = out["miKnn"].cpu().numpy()
+        gd2 = out["d2Knn"].cpu().numpy()
+        # ties among the blob are resolved by index in both forms
+        blob = slice(990, 1420)
+        assert np.array_equal(got[blob], idx[blob]), mode
+        assert np.array_equal(gd2[blob].view(np.int32), d2[blob].view(np.int32)), mode
+        # elsewhere BF16 may re-order FP32 near-ties by their FP64 distance
+        same = np.all(got == idx, axis=1).mean()
+        assert same == 1.0 if mode == "exact" else same >= 0.995, (mode, same)
+
+
 @pytest.mark.parametrize("case", CASES[:3] + CASES[4:])
 def test_bf16_delta_vs_fp64(gpu, case):
     F, plan, _ = small_site(**case)
