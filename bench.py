@@ -196,6 +196,12 @@ def run_ours(args):
     e2e = None
     if not results.get(head, {}).get("error"):
         e2e = time_e2e(P, site["F"], head, args, dev, torch, irc, world, dist if world > 1 else None)
+    batched = None
+    if args.batched and rank == 0:
+        del F
+        P.close()
+        batched = run_batched(args, dev, torch, irc, flush, stream)
+        P = None
 
     out = None
     if rank == 0:
@@ -236,13 +242,75 @@ def run_ours(args):
             "roofline": roof,
             "gpu_launches": n_launch.get(head, 0) * args.steps,
         }
+        if batched is not None:
+            out["batched"] = batched
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(site, plan, seconds=args.cpu_seconds)
-    P.close()
+    if P is not None:
+        P.close()
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
     return out
+
+
+def run_batched(args, dev, torch, irc, flush, stream):
+    """The probe-scale batch (384 sites, 10M spikes, D in {18, 24, 33}, 1,200
+    drift chunks): all sites in one plan, one launch per kernel, the whole
+    kNN + rho + delta sequence captured in a CUDA graph and replayed."""
+    from ironclust_gb300 import synth
+    from ironclust_gb300.drift import plan_pairs
+    t0 = time.perf_counter()
+    b, specs = synth.make_probe(n_sites=args.probe_sites, total=args.probe_spikes)
+    gen_s = time.perf_counter() - t0
+    N = b.F.shape[0]
+    F = torch.from_numpy(b.F).to(dev)
+    P = irc.Plan(b.plan)
+    res = {"workload": "probe10m" if args.probe_sites == 384 else "probe%d" % args.probe_sites,
+           "sites": b.n_sites, "spikes": N, "chunks": int(len(b.plan["q0"])), "pairs": plan_pairs(b.plan),
+           "dims": sorted(set(int(d) for d in b.dims)), "generation_s": gen_s, "forms": {}}
+    outs = {}
+    for mode in [m.strip() for m in args.batched_forms.split(",") if m.strip()]:
+        for _ in range(2):
+            irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
+        torch.cuda.synchronize()
+        eager = []
+        for _ in range(args.batched_steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
+            e1.record(stream)
+            e1.synchronize()
+            eager.append(e0.elapsed_time(e1))
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)      # warm on the capture stream
+        torch.cuda.current_stream().wait_stream(side)
+        with torch.cuda.graph(g, capture_error_mode="relaxed"):
+            out = irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
+        graph = []
+        for _ in range(args.batched_steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
+            e1.synchronize()
+            graph.append(e0.elapsed_time(e1))
+        ms_e, ms_g = sum(eager) / len(eager), sum(graph) / len(graph)
+        res["forms"][mode] = {"ms_eager": ms_e, "ms_graph": ms_g, "spikes_per_s_graph": N / (ms_g / 1e3),
+                              "spikes_per_s_eager": N / (ms_e / 1e3)}
+        outs[mode] = out["miKnn"].clone()
+        del g
+    if "exact" in outs:
+        for mode, mi in outs.items():
+            if mode != "exact":
+                res["forms"][mode]["recall_vs_exact"] = knn_recall(outs["exact"], mi, torch)
+    P.close()
+    return res
 
 
 def knn_recall(ref, got, torch):
@@ -387,6 +455,13 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-chunks", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched", dest="batched", action="store_true", default=True,
+                    help="also time the probe-scale batch (all sites in one plan, CUDA graph)")
+    ap.add_argument("--no-batched", dest="batched", action="store_false")
+    ap.add_argument("--batched-forms", default="bf16,exact")
+    ap.add_argument("--batched-steps", type=int, default=3)
+    ap.add_argument("--probe-sites", type=int, default=384)
+    ap.add_argument("--probe-spikes", type=int, default=10_000_000)
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -1,0 +1,53 @@
+"""All probe sites as one batch: one feature matrix, one plan, one launch per kernel.
+
+IronClust processes sites one by one in a parfor (matlab/irc2.m:3539-3561),
+each site with its own feature dimension.  Here the sites of a probe are
+stacked into one feature matrix, zero-padded to the largest dimension, and
+their per-chunk launch plans are concatenated with row offsets.  A padded
+feature is 0 for every spike of its site, so it adds exactly 0 to each fused
+accumulate: every distance, and so every result, equals the per-site one
+bit for bit.  Candidate runs never cross sites, so the batch is a plan like
+any other and runs through irc_plan_create / irc_site_knn / irc_site_delta
+in one launch per kernel; the tensor-core kernel packs the small chunks of
+many sites into shared CTAs.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .drift import build_plan
+
+
+class SiteBatch:
+    """sites: iterable of dict(F [n, D] float32, viDrift [n], mlDrift [nDrift x nDrift])."""
+
+    def __init__(self, sites):
+        sites = list(sites)
+        self.n_sites = len(sites)
+        self.dims = np.array([s["F"].shape[1] for s in sites], np.int32)
+        self.sizes = np.array([s["F"].shape[0] for s in sites], np.int64)
+        self.bases = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        n, dmax = int(self.bases[-1]), int(self.dims.max())
+        self.F = np.zeros((n, dmax), np.float32)
+        q0, nq, rs, rn, roff, site_of_chunk = [], [], [], [], [0], []
+        for i, s in enumerate(sites):
+            b = int(self.bases[i])
+            self.F[b:b + s["F"].shape[0], :s["F"].shape[1]] = s["F"]
+            p = build_plan(s["viDrift"], np.ones(s["F"].shape[0], bool), s["mlDrift"])
+            q0.append(p["q0"] + b)
+            nq.append(p["nq"])
+            rs.append(p["rs"] + b)
+            rn.append(p["rn"])
+            roff.extend((p["roff"][1:] + roff[-1]).tolist())
+            site_of_chunk.append(np.full(len(p["q0"]), i, np.int32))
+        i32 = lambda parts: np.concatenate(parts).astype(np.int32)
+        self.plan = dict(q0=i32(q0), nq=i32(nq), roff=np.asarray(roff, np.int32), rs=i32(rs), rn=i32(rn),
+                         q_base=0, n_out=n, n_f=n)
+        self.site_of_chunk = np.concatenate(site_of_chunk)
+
+    def site_slice(self, i):
+        return slice(int(self.bases[i]), int(self.bases[i + 1]))
+
+    def split_knn(self, miKnn, i):
+        """kNN rows of site i with indices local to that site (1-based)."""
+        return np.asarray(miKnn)[self.site_slice(i)] - int(self.bases[i])

@@ -591,6 +591,7 @@ extern "C" int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t 
     IRC_CHECK_LAUNCH("irc_site_knn_exact_noalloc tiles");
     irc::PlanDev p;
     p.q0 = d_q0; p.nq = d_nq; p.roff = d_roff; p.rs = d_rs; p.rn = d_rn;
+    p.roffr = d_roff; p.rsr = d_rs; p.rnr = d_rn;         // the EXACT kernels take any run split
     for (int k = 0; k < irc::kNumTileSizes; ++k) p.tile_off[k] = d_tile;     // only the 16-query table is read
     p.nChunks = nChunks; p.q_base = q_base; p.n_out = n_out; p.nF = nF; p.nRuns = nRuns;
     const size_t smem = (size_t)kQB * kCap * 8 + (size_t)kQB * kThreads * 4;

@@ -20,9 +20,25 @@ __host__ __device__ constexpr int tile_slot(int qb)
     return qb == 8 ? 0 : qb == 16 ? 1 : qb == 32 ? 2 : qb == 64 ? 3 : 4;
 }
 
+// Work item of the tensor-core kNN: up to four slots packed into one 128-row
+// tile; slot s covers queries [qs[s], qs[s]+nq[s]) of chunk[s] (chunk < 0:
+// empty) and 128/nslot rows of the tile.
+struct TcItem {
+    int nslot;
+    int chunk[4];
+    int qs[4];
+    int nq[4];
+    int pad[3];
+};
+static_assert(sizeof(TcItem) == 64, "TcItem is 16 words");
+
 // Plain device pointers into one allocation owned by irc_plan.
+// roff/rs/rn: every chunk's candidate set as maximal contiguous row intervals
+// (adjacent linked runs merged); roffr/rsr/rnr: the runs exactly as the
+// reference passes them (IBB/NBB), which the REF kernels' bins depend on.
 struct PlanDev {
     const int32_t *q0, *nq, *roff, *rs, *rn;
+    const int32_t *roffr, *rsr, *rnr;
     const int32_t *tile_off[kNumTileSizes];   // [nChunks+1] prefix sums of ceil(nq/QB)
     int nChunks, q_base, n_out, nF, nRuns;
 };
@@ -49,6 +65,8 @@ struct irc_plan {
     irc::PlanDev dev;
     void *dmem;                            // single device allocation behind dev
     int32_t *scratch;                      // inside dmem: 4 words + 2 x n_out query lists
+    const irc::TcItem *tc_items;           // inside dmem: tensor-core work items, largest first
+    int n_tc_items;
     void *tc_buf;                          // tensor-core operand rows (2 x nF x tc_row_bytes), lazily
     size_t tc_row_bytes;
     int ntiles[irc::kNumTileSizes];        // host copy of tile counts

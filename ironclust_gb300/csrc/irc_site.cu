@@ -9,6 +9,7 @@
 // device with warp arg-min reductions over (value, bin) keys -- the stable
 // ascending order of MATLAB's sort.  Results equal the reference kernels +
 // MATLAB post-processing bit for bit.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -35,13 +36,13 @@ k_site_knn_ref(irc::PlanDev p, const float *__restrict__ F, int nC, int nT, int 
     int *sI = reinterpret_cast<int *>(sV + QB * nT);       // [QB][nT]  1-based index
     int chunk, qs, n;
     irc::tile_lookup<QB>(p, blockIdx.x, chunk, qs, n);
-    const int r0 = __ldg(p.roff + chunk), nBB = __ldg(p.roff + chunk + 1) - r0;
+    const int r0 = __ldg(p.roffr + chunk), nBB = __ldg(p.roffr + chunk + 1) - r0;
     irc::stage_queries<QB>(F, nC, qs, n, sA);
     __syncthreads();
     const int nT0 = nT / nBB;
     for (int t = threadIdx.x; t < nT; t += blockDim.x) {
         const int b = t % nBB;
-        const int ib0 = __ldg(p.rs + r0 + b), nb0 = __ldg(p.rn + r0 + b);
+        const int ib0 = __ldg(p.rsr + r0 + b), nb0 = __ldg(p.rnr + r0 + b);
         float mn[QB];
         int mi[QB];
 #pragma unroll
@@ -95,7 +96,7 @@ k_site_delta_ref(irc::PlanDev p, const float *__restrict__ F, const float *__res
     __shared__ int sIdx[QB][kThreads / 32];
     int chunk, qs, n;
     irc::tile_lookup<QB>(p, blockIdx.x, chunk, qs, n);
-    const int r0 = __ldg(p.roff + chunk), nBB = __ldg(p.roff + chunk + 1) - r0;
+    const int r0 = __ldg(p.roffr + chunk), nBB = __ldg(p.roffr + chunk + 1) - r0;
     irc::stage_queries<QB>(F, nC, qs, n, sA);
     if (threadIdx.x < QB) sRA[threadIdx.x] = __ldg(R + qs + min((int)threadIdx.x, n - 1));
     __syncthreads();
@@ -106,7 +107,7 @@ k_site_delta_ref(irc::PlanDev p, const float *__restrict__ F, const float *__res
     for (int q = 0; q < QB; ++q) { bk[q] = ~0ull; bi[q] = 0; }
     for (int t = threadIdx.x; t < nT; t += blockDim.x) {
         const int b = t % nBB;
-        const int ib0 = __ldg(p.rs + r0 + b), nb0 = __ldg(p.rn + r0 + b);
+        const int ib0 = __ldg(p.rsr + r0 + b), nb0 = __ldg(p.rnr + r0 + b);
         float mn[QB];
         int mi[QB];
 #pragma unroll
@@ -146,6 +147,64 @@ k_site_delta_ref(irc::PlanDev p, const float *__restrict__ F, const float *__res
 }
 
 inline int tiles_for(const irc_plan *pl, int qb) { return pl->ntiles[irc::tile_slot(qb)]; }
+
+struct Slot {
+    int chunk, qs, nq, nt;
+};
+
+// Work items of the tensor-core kNN (see irc_tc.cu).  Cost of an item: the
+// largest candidate-tile count among its slots (its slots run side by side).
+std::vector<irc::TcItem> build_tc_items(const int32_t *q0, const int32_t *nq, const int32_t *roff,
+                                        const int32_t *rn, int nChunks)
+{
+    std::vector<irc::TcItem> items;
+    std::vector<int> cost;
+    std::vector<Slot> s2, s1;
+    auto push = [&](int nslot, const Slot *sl, int n) {
+        irc::TcItem it;
+        memset(&it, 0, sizeof(it));
+        it.nslot = nslot;
+        int c = 0;
+        for (int s = 0; s < 4; ++s) {
+            it.chunk[s] = s < n ? sl[s].chunk : -1;
+            it.qs[s] = s < n ? sl[s].qs : 0;
+            it.nq[s] = s < n ? sl[s].nq : 0;
+            if (s < n) c = std::max(c, sl[s].nt);
+        }
+        items.push_back(it);
+        cost.push_back(c);
+    };
+    for (int i = 0; i < nChunks; ++i) {
+        int nt = 0;
+        for (int r = roff[i]; r < roff[i + 1]; ++r) nt += (rn[r] + 127) / 128;
+        int q = q0[i], R = nq[i];
+        while (R > 64) {
+            const Slot s{i, q, std::min(128, R), nt};
+            push(1, &s, 1);
+            q += s.nq;
+            R -= s.nq;
+        }
+        if (R > 32) s2.push_back(Slot{i, q, R, nt});
+        else if (R > 0) s1.push_back(Slot{i, q, R, nt});
+    }
+    auto by_nt = [](const Slot &a, const Slot &b) { return a.nt > b.nt || (a.nt == b.nt && a.chunk < b.chunk); };
+    std::sort(s2.begin(), s2.end(), by_nt);
+    std::sort(s1.begin(), s1.end(), by_nt);
+    for (size_t k = 0; k < s2.size(); k += 2) push(2, &s2[k], (int)std::min<size_t>(2, s2.size() - k));
+    for (size_t k = 0; k < s1.size(); k += 4) push(4, &s1[k], (int)std::min<size_t>(4, s1.size() - k));
+    std::vector<int> order(items.size());
+    for (size_t k = 0; k < order.size(); ++k) order[k] = (int)k;
+    // largest first; items of one chunk stay adjacent so the CTAs that stream
+    // the same candidate tiles run together and share them in L2
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (cost[a] != cost[b]) return cost[a] > cost[b];
+        return items[a].chunk[0] < items[b].chunk[0];
+    });
+    std::vector<irc::TcItem> out;
+    out.reserve(items.size());
+    for (int k : order) out.push_back(items[k]);
+    return out;
+}
 
 }  // namespace
 
@@ -232,9 +291,21 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     img.reserve(4 * nCh + 2 * nRuns + irc::kNumTileSizes * (nCh + 1) + 8);
     size_t off_q0 = img.size(); img.insert(img.end(), q0, q0 + nCh);
     size_t off_nq = img.size(); img.insert(img.end(), nq, nq + nCh);
-    size_t off_roff = img.size(); img.insert(img.end(), roff, roff + nCh + 1);
-    size_t off_rs = img.size(); img.insert(img.end(), rs, rs + nRuns);
-    size_t off_rn = img.size(); img.insert(img.end(), rn, rn + nRuns);
+    // candidate intervals: adjacent runs of a chunk merged (same candidate set)
+    std::vector<int32_t> moff(1, 0), ms, mn;
+    for (int i = 0; i < nChunks; ++i) {
+        for (int r = roff[i]; r < roff[i + 1]; ++r) {
+            if ((int)ms.size() > moff.back() && ms.back() + mn.back() == rs[r]) mn.back() += rn[r];
+            else { ms.push_back(rs[r]); mn.push_back(rn[r]); }
+        }
+        moff.push_back((int32_t)ms.size());
+    }
+    size_t off_roff = img.size(); img.insert(img.end(), moff.begin(), moff.end());
+    size_t off_rs = img.size(); img.insert(img.end(), ms.begin(), ms.end());
+    size_t off_rn = img.size(); img.insert(img.end(), mn.begin(), mn.end());
+    size_t off_roffr = img.size(); img.insert(img.end(), roff, roff + nCh + 1);
+    size_t off_rsr = img.size(); img.insert(img.end(), rs, rs + nRuns);
+    size_t off_rnr = img.size(); img.insert(img.end(), rn, rn + nRuns);
     size_t off_tile[irc::kNumTileSizes];
     for (int k = 0; k < irc::kNumTileSizes; ++k) {
         const int qb = irc::kTileSizes[k];
@@ -243,6 +314,16 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
         img.push_back(0);
         for (int i = 0; i < nChunks; ++i) { acc += (nq[i] + qb - 1) / qb; img.push_back(acc); }
         pl->ntiles[k] = acc;
+    }
+    // tensor-core work items: 128-row tiles of large chunks, then the 33-64 and
+    // 1-32 row remainders packed two and four per item (similar tile counts
+    // together), all ordered by cost, largest first
+    std::vector<irc::TcItem> items = build_tc_items(q0, nq, moff.data(), mn.data(), nChunks);
+    while (img.size() % 16) img.push_back(0);
+    const size_t off_items = img.size();
+    for (const irc::TcItem &it : items) {
+        const int32_t *w = reinterpret_cast<const int32_t *>(&it);
+        img.insert(img.end(), w, w + 16);
     }
     cudaGetDevice(&pl->device);
     if (img.size() & 1) img.push_back(0);          // scratch starts 8-byte aligned (int2 items)
@@ -263,15 +344,20 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     pl->dev.roff = base + off_roff;
     pl->dev.rs = base + off_rs;
     pl->dev.rn = base + off_rn;
+    pl->dev.roffr = base + off_roffr;
+    pl->dev.rsr = base + off_rsr;
+    pl->dev.rnr = base + off_rnr;
     for (int k = 0; k < irc::kNumTileSizes; ++k) pl->dev.tile_off[k] = base + off_tile[k];
     pl->scratch = (int32_t *)pl->dmem + img.size();
+    pl->tc_items = reinterpret_cast<const irc::TcItem *>((const int32_t *)pl->dmem + off_items);
+    pl->n_tc_items = (int)items.size();
     e = cudaMemset(pl->scratch, 0, irc::kScratchLists * sizeof(int32_t));      // counters and error word
     if (e != cudaSuccess) { cudaFree(pl->dmem); free(pl); return irc_host::cuda_status(e, "irc_plan_create: clear"); }
     pl->dev.nChunks = nChunks;
     pl->dev.q_base = q_base;
     pl->dev.n_out = n_out;
     pl->dev.nF = nF;
-    pl->dev.nRuns = nRuns;
+    pl->dev.nRuns = (int)ms.size();
     pl->max_nq = max_nq;
     pl->pairs = pairs;
     *out = pl;

@@ -1,23 +1,26 @@
 // irc_tc.cu -- tensor-core (tcgen05) site kNN: BF16 distance filter, exact
 // FP32 re-rank, FP64 at the k-th-neighbour boundary.
 //
-// Per CTA: 128 queries of one drift chunk (TMEM lanes) against every linked
-// candidate, in 128-candidate tiles (TMEM columns, two accumulator
-// buffers).  The BF16 operand rows (see irc_tc_host.cu) make every
+// A CTA serves one work item: up to four "slots", each a run of queries of
+// one drift chunk (128, 64 or 32 rows), packed into the 128 TMEM lanes of
+// one M=128 tile; every slot owns a share of the four 128-column TMEM
+// accumulators and its own epilogue warps, and the slots' candidate tiles
+// are issued round-robin so small chunks (a probe site has ~17 queries per
+// chunk) share a CTA without waiting on each other.  Items are ordered by
+// cost, largest first.  The BF16 operand rows (irc_tc_host.cu) make every
 // accumulator the approximate squared distance.  Warp roles: warp 0 issues
-// TMA loads (4-stage ring), warp 1 owns TMEM and issues tcgen05.mma from one
-// thread, warps 2-9 are the epilogue: two warps per TMEM lane quarter, each
-// owning one half (64 columns) of every tile, so a query is served by two
-// threads.  The candidate tiles are streamed twice:
-//   pass 1  every thread folds its half-tiles into 64 per-column minima (one
+// TMA loads (4-stage ring of 128-candidate tiles, four 32-row query boxes),
+// warp 1 owns TMEM and issues tcgen05.mma from one thread, warps 2-17 are
+// the epilogue: four per TMEM lane quarter, each reading 32 columns of
+// every tile of its slot.  Each slot's candidate tiles are streamed twice:
+//   pass 1  every thread folds its columns into 32 per-column minima (one
 //           FMNMX per pair, no branches); per query, the 64th smallest of the
-//           128 minima of both halves is an upper bound tau on the 64th
-//           nearest approximate distance (64 distinct candidates lie at or
-//           below it);
+//           128 minima is an upper bound tau on the 64th nearest approximate
+//           distance (64 distinct candidates lie at or below it);
 //   pass 2  every thread marks the pairs at or below tau in a 32-bit mask
 //           (one compare and one predicated OR per pair) and appends only the
-//           marked candidates to its half-list in shared memory (~90 per
-//           query on random data; 96 per half; an overflowing query is
+//           marked candidates to its part-list in shared memory (~90 per
+//           query on random data, 64 per part; an overflowing query is
 //           finished by the exact fallback kernel).
 // Every listed candidate is then re-ranked with the reference FP32
 // arithmetic (exact), zero distances dropped, sorted by (distance, index)
@@ -47,7 +50,8 @@ constexpr int EPI_WARPS = 4 * PARTS;
 constexpr int EPI_THREADS = 32 * EPI_WARPS;
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TILE_BYTES = BN * KP * 2;      // 16 KB (A tile has the same size)
-constexpr uint32_t TMEM_COLS = 2 * BN;
+constexpr int NBUF = 4;                           // TMEM accumulator buffers, split among the slots
+constexpr uint32_t TMEM_COLS = NBUF * BN;         // all 512 columns (one CTA per SM)
 constexpr size_t LIST_BYTES = (size_t)LROWP * PARTS * BM * 4;
 constexpr int WARP_KEYS = 64;                     // sorted re-rank keys kept per epilogue warp
 constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + TILE_BYTES * (1 + STAGES) + LIST_BYTES +
@@ -190,12 +194,291 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const
     __syncwarp();
 }
 
-__device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory"); }
+__device__ __forceinline__ void slot_barrier(int slot, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + slot), "r"(nthreads) : "memory");
+}
+
+// Cursor over the candidate tiles of one chunk: run r (absolute index), offset t.
+struct TileCursor {
+    int r, r0, r1, t, rs, rn;                     // run bounds cached per run
+    __device__ __forceinline__ void load(const irc::PlanDev &p)
+    {
+        rs = __ldg(p.rs + r);
+        rn = __ldg(p.rn + r);
+    }
+    __device__ __forceinline__ void reset(const irc::PlanDev &p, int chunk)
+    {
+        r0 = __ldg(p.roff + chunk);
+        r1 = __ldg(p.roff + chunk + 1);
+        r = r0;
+        t = 0;
+        load(p);
+    }
+    // current tile: first candidate row and valid column count; then advance
+    __device__ __forceinline__ void next(const irc::PlanDev &p, int &row0, int &ncol)
+    {
+        row0 = rs + t;
+        ncol = min(BN, rn - t);
+        t += BN;
+        if (t >= rn) {                                // next run; wraps for the second pass
+            t = 0;
+            if (++r >= r1) r = r0;
+            load(p);
+        }
+    }
+};
+
+__device__ __forceinline__ int chunk_tiles(const irc::PlanDev &p, int chunk)
+{
+    if (chunk < 0) return 0;
+    int n = 0;
+    for (int r = __ldg(p.roff + chunk); r < __ldg(p.roff + chunk + 1); ++r) n += (__ldg(p.rn + r) + BN - 1) / BN;
+    return n;
+}
+
+// Epilogue of one warp: lane quarter `quarter` (the TMEM lanes it may read),
+// 32 columns `part` of every tile of its slot.  Each slot's epilogue warps
+// synchronise only among themselves (named barrier 1 + slot).
+__device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::TcItem &it, const int (&nt)[4], int qps,
+                                         int bps, uint32_t tmem, uint32_t *lists, unsigned long long *wkeys,
+                                         float *sTau, int *sCnt, uint64_t *acc_full, uint64_t *acc_empty,
+                                         volatile int *abort_flag, const float *__restrict__ F, int nC, int knn,
+                                         float *vrKnn, float *rho, int *miKnn, float *d2Knn, int *scratch, int warp,
+                                         int lane)
+{
+    const int ew = warp - 2;                      // 0..15
+    const int quarter = warp & 3;                 // TMEM lane quarter this warp may access
+    const int part = ew >> 2;                     // which 32 columns of every tile
+    const int s = quarter / qps;                  // slot of this lane quarter
+    const int qrow = (quarter % qps) * 32;        // first row of this quarter inside its slot
+    const int nq_s = it.chunk[s] >= 0 ? it.nq[s] : 0;
+    const int nts = nt[s];
+    const int slot_threads = 32 * PARTS * qps;
+    const int row = quarter * 32 + lane;
+    const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + part * PART;
+    const bool active = qrow < nq_s;              // warp-uniform: any valid query in this quarter
+    bool ok = true;
+    TileCursor cur;
+    if (nts) cur.reset(p, it.chunk[s]);
+
+    // pass 1: per-column minima of this part
+    float bm[PART];
+#pragma unroll
+    for (int c = 0; c < PART; ++c) bm[c] = __int_as_float(0x7f800000);
+    int bj = 0, use = 0;                          // tile j of this slot: buffer s*bps + bj, use count
+    for (int j = 0; j < nts && ok; ++j) {
+        const int b = s * bps + bj;
+        const uint32_t par = use & 1;
+        if (++bj == bps) { bj = 0; ++use; }
+        int row0, ncol;
+        cur.next(p, row0, ncol);
+        if (!(ok = sm100::mbar_wait(&acc_full[b], par, abort_flag))) break;
+        sm100::tc_fence_after();
+        const int lim = ncol - part * PART;                   // valid columns in this part
+        if (active && lim > 0) {
+            float v[32];
+            sm100::tmem_ld32(tbase + b * BN, v);
+            if (lim >= 32) {
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) bm[jj] = fminf(bm[jj], v[jj]);
+            } else {
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj)
+                    if (jj < lim) bm[jj] = fminf(bm[jj], v[jj]);
+            }
+        }
+        sm100::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
+    }
+    // threshold: 64th smallest of the 128 column minima of every query; the
+    // minima rows of a quarter alias that quarter's own list rows
+    float *qarea = reinterpret_cast<float *>(lists + (size_t)quarter * 32 * PARTS * LROWP);
+    {
+        float *brow = qarea + lane * BROW + part * PART;
+#pragma unroll
+        for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
+        slot_barrier(s, slot_threads);
+        for (int L = 0; L < 32 / PARTS; ++L) {
+            const int rl = part * (32 / PARTS) + L;            // row inside the quarter
+            const float *bl = qarea + rl * BROW;
+            unsigned v4[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v4[u] = __float_as_uint(bl[u * 32 + lane]);
+            warp_bitonic<unsigned, 4>(v4, lane);
+            const unsigned kth = __shfl_sync(0xffffffffu, v4[63 % 4], 63 / 4);
+            if (lane == 0) sTau[quarter * 32 + rl] = __uint_as_float(kth);
+        }
+        slot_barrier(s, slot_threads);     // minima rows are read; the list rows may be written
+    }
+    const float tau = sTau[row];
+    // pass 2: collect the candidates at or below tau
+    uint32_t *lrow = lists + ((size_t)row * PARTS + part) * LROWP;
+    int cnt = 0;
+    bool ovf = false;
+    for (int j = nts; j < 2 * nts && ok; ++j) {
+        const int b = s * bps + bj;
+        const uint32_t par = use & 1;
+        if (++bj == bps) { bj = 0; ++use; }
+        int row0, ncol;
+        cur.next(p, row0, ncol);
+        if (!(ok = sm100::mbar_wait(&acc_full[b], par, abort_flag))) break;
+        sm100::tc_fence_after();
+        const int lim = ncol - part * PART;
+        if (active && lim > 0) {
+            float v[32];
+            sm100::tmem_ld32(tbase + b * BN, v);
+            unsigned m = 0;
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj)
+                if (v[jj] <= tau) m |= 1u << jj;
+            if (lim < 32) m &= (1u << lim) - 1u;
+            if (cnt + __popc(m) > CAPP) { ovf = true; m = 0; }
+            const uint32_t c0 = (uint32_t)(row0 + part * PART);
+            while (m) {
+                const int jj = __ffs(m) - 1;
+                m &= m - 1u;
+                lrow[cnt++] = c0 + (uint32_t)jj;
+            }
+        }
+        sm100::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
+    }
+    sCnt[row * PARTS + part] = ovf ? -1 : cnt;
+    slot_barrier(s, slot_threads);
+    // exact re-rank: this warp serves 8 of its quarter's queries
+    unsigned long long *ws = wkeys + (size_t)ew * WARP_KEYS;
+    for (int L = 0; L < 32 / PARTS && ok; ++L) {
+        const int rl = part * (32 / PARTS) + L;
+        if (qrow + rl >= nq_s) break;
+        const int rowL = quarter * 32 + rl;
+        const int q = it.qs[s] + qrow + rl;
+        int c[PARTS];
+        bool over = false;
+#pragma unroll
+        for (int u = 0; u < PARTS; ++u) { c[u] = sCnt[rowL * PARTS + u]; over |= c[u] < 0; }
+        if (over) {                                   // finished by the exact fallback kernel
+            if (lane == 0) {
+                const int k = atomicAdd(scratch + 0, 1);
+                scratch[irc::kScratchLists + k] = q;
+            }
+            continue;
+        }
+        const int cL = c[0] + c[1] + c[2] + c[3];
+        const uint32_t *lr = lists + (size_t)rowL * PARTS * LROWP;
+        const size_t o = (size_t)(q - p.q_base);
+        if (cL <= 64)
+            rerank<2>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        else if (cL <= 128)
+            rerank<4>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        else
+            rerank<8>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+    }
+}
+
+// TMA producer (one thread): the four 32-row query boxes, then the slots'
+// candidate tiles round-robin, each slot's sequence twice (both passes).
+template <int NS>
+__device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMap &tmC, const irc::PlanDev &p,
+                                        const irc_tc::TcItem &it, const int (&nt)[4], uint8_t *sA, uint8_t *sB,
+                                        uint64_t *full, uint64_t *empty, uint64_t *a_full, volatile int *abort_flag)
+{
+    constexpr int QPS = 4 / NS;
+    sm100::prefetch_tmap(&tmQ);
+    sm100::prefetch_tmap(&tmC);
+    sm100::mbar_arrive_expect_tx(a_full, TILE_BYTES);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int s = q / QPS;
+        const int row0 = it.chunk[s] >= 0 ? it.qs[s] + (q % QPS) * 32 : 0;
+        sm100::tma_load_2d(&tmQ, a_full, sA + q * (TILE_BYTES / 4), 0, row0);
+    }
+    TileCursor cur[NS];
+    int n2[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        n2[s] = 2 * nt[s];
+        if (nt[s]) cur[s].reset(p, it.chunk[s]);
+    }
+    int i = 0;
+    bool ok = true;
+    for (int k = 0; ok; ++k) {
+        bool any = false;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            if (ok && k < n2[s]) {
+                any = true;
+                int row0, ncol;
+                cur[s].next(p, row0, ncol);
+                const int st = i % STAGES;
+                if ((ok = sm100::mbar_wait(&empty[st], ((i / STAGES) & 1) ^ 1, abort_flag))) {
+                    sm100::mbar_arrive_expect_tx(&full[st], TILE_BYTES);
+                    sm100::tma_load_2d(&tmC, &full[st], sB + (size_t)st * TILE_BYTES, 0, row0);
+                    ++i;
+                }
+            }
+        }
+        if (!any) break;
+    }
+    // every issued load has landed before the CTA exits
+    for (int j = (i > STAGES ? i - STAGES : 0); j < i; ++j)
+        sm100::mbar_wait(&full[j % STAGES], (j / STAGES) & 1, abort_flag);
+    sm100::mbar_wait(a_full, 0, abort_flag);
+}
+
+// MMA issuer (one thread), in the producer's order; slot s's tile k goes to
+// accumulator s*BPS + k % BPS.
+template <int NS>
+__device__ __forceinline__ void issue(const int (&nt)[4], uint32_t tmem, uint8_t *sA, uint8_t *sB, uint64_t *full,
+                                      uint64_t *empty, uint64_t *a_full, uint64_t *acc_full, uint64_t *acc_empty,
+                                      uint64_t *mma_done, volatile int *abort_flag)
+{
+    constexpr int BPS = NBUF / NS;
+    constexpr uint32_t idesc = sm100::idesc_make(BM, BN, 1, 1);   // bf16 x bf16 -> f32
+    if (sm100::mbar_wait(a_full, 0, abort_flag)) {
+        sm100::tc_fence_after();
+        const uint64_t adesc = sm100::sdesc_sw128(sm100::smem_u32(sA));
+        int n2[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) n2[s] = 2 * nt[s];
+        int i = 0;
+        bool ok = true;
+        for (int k = 0; ok; ++k) {
+            bool any = false;
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                if (ok && k < n2[s]) {
+                    any = true;
+                    const int b = s * BPS + k % BPS, u = k / BPS, st = i % STAGES;
+                    ok = sm100::mbar_wait(&acc_empty[b], (u & 1) ^ 1, abort_flag) &&
+                         sm100::mbar_wait(&full[st], (i / STAGES) & 1, abort_flag);
+                    if (ok) {
+                        sm100::tc_fence_after();
+                        const uint64_t bdesc = sm100::sdesc_sw128(sm100::smem_u32(sB + (size_t)st * TILE_BYTES));
+#pragma unroll
+                        for (int kk = 0; kk < KP / 16; ++kk)
+                            sm100::mma_f16(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
+                        sm100::mma_commit(&empty[st]);
+                        sm100::mma_commit(&acc_full[b]);
+                        ++i;
+                    }
+                }
+            }
+            if (!any) break;
+        }
+    }
+    // every MMA has completed before TMEM is released
+    sm100::mma_commit(mma_done);
+    sm100::mbar_wait(mma_done, 0, abort_flag);
+}
 
 __global__ void __launch_bounds__(THREADS, 1)
 k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
-              const float *__restrict__ F, int nC, int knn, float *__restrict__ vrKnn, float *__restrict__ rho,
-              int *__restrict__ miKnn, float *__restrict__ d2Knn, int *__restrict__ scratch)
+              const irc_tc::TcItem *__restrict__ items, const float *__restrict__ F, int nC, int knn,
+              float *__restrict__ vrKnn, float *__restrict__ rho, int *__restrict__ miKnn,
+              float *__restrict__ d2Knn, int *__restrict__ scratch)
 {
     extern __shared__ unsigned char smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -207,21 +490,24 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
     int *sCnt = reinterpret_cast<int *>(sTau + BM);                                  // [BM][PARTS], -1 = overflow
     uint64_t *bars = reinterpret_cast<uint64_t *>(sCnt + PARTS * BM);
     uint64_t *full = bars, *empty = bars + STAGES, *a_full = bars + 2 * STAGES;
-    uint64_t *acc_full = a_full + 1, *acc_empty = a_full + 3, *mma_done = a_full + 5;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(a_full + 6);
+    uint64_t *acc_full = a_full + 1, *acc_empty = acc_full + NBUF, *mma_done = acc_empty + NBUF;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int chunk, qs, nq;
-    irc::tile_lookup<BM>(p, blockIdx.x, chunk, qs, nq);
-    const int r0 = __ldg(p.roff + chunk), r1 = __ldg(p.roff + chunk + 1);
-    int ntiles = 0;
-    for (int r = r0; r < r1; ++r) ntiles += (__ldg(p.rn + r) + BN - 1) / BN;
+    const irc_tc::TcItem it = items[blockIdx.x];
+    const int nslot = it.nslot, qps = 4 / nslot, bps = NBUF / nslot;
+    int nt[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) nt[s] = s < nslot ? chunk_tiles(p, it.chunk[s]) : 0;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) { sm100::mbar_init(&full[s], 1); sm100::mbar_init(&empty[s], 1); }
         sm100::mbar_init(a_full, 1);
-        for (int b = 0; b < 2; ++b) { sm100::mbar_init(&acc_full[b], 1); sm100::mbar_init(&acc_empty[b], EPI_WARPS); }
+        for (int b = 0; b < NBUF; ++b) {
+            sm100::mbar_init(&acc_full[b], 1);
+            sm100::mbar_init(&acc_empty[b], PARTS * qps);      // the owning slot's epilogue warps
+        }
         sm100::mbar_init(mma_done, 1);
         *abort_flag = 0;
         sm100::fence_mbar_init();
@@ -233,172 +519,21 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0) {
-        // ---------------- TMA producer: the tile sequence, twice ----------------
         if (lane == 0) {
-            sm100::prefetch_tmap(&tmQ);
-            sm100::prefetch_tmap(&tmC);
-            sm100::mbar_arrive_expect_tx(a_full, TILE_BYTES);
-            sm100::tma_load_2d(&tmQ, a_full, sA, 0, qs);
-            int i = 0;
-            bool ok = true;
-            for (int pass = 0; pass < 2 && ok; ++pass)
-                for (int r = r0; r < r1 && ok; ++r) {
-                    const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
-                    for (int t = 0; t < rn; t += BN, ++i) {
-                        const int s = i % STAGES;
-                        if (!(ok = sm100::mbar_wait(&empty[s], ((i / STAGES) & 1) ^ 1, abort_flag))) break;
-                        sm100::mbar_arrive_expect_tx(&full[s], TILE_BYTES);
-                        sm100::tma_load_2d(&tmC, &full[s], sB + (size_t)s * TILE_BYTES, 0, rs + t);
-                    }
-                }
-            // every issued load has landed before the CTA exits
-            for (int j = (i > STAGES ? i - STAGES : 0); j < i; ++j)
-                sm100::mbar_wait(&full[j % STAGES], (j / STAGES) & 1, abort_flag);
-            sm100::mbar_wait(a_full, 0, abort_flag);
+            if (nslot == 1) produce<1>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+            else if (nslot == 2) produce<2>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+            else produce<4>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
         }
     } else if (warp == 1) {
-        // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t idesc = sm100::idesc_make(BM, BN, 1, 1);   // bf16 x bf16 -> f32
-            if (sm100::mbar_wait(a_full, 0, abort_flag)) {
-                sm100::tc_fence_after();
-                const uint64_t adesc = sm100::sdesc_sw128(sm100::smem_u32(sA));
-                for (int i = 0; i < 2 * ntiles; ++i) {
-                    const int s = i % STAGES, b = i & 1;
-                    if (!sm100::mbar_wait(&acc_empty[b], ((i >> 1) & 1) ^ 1, abort_flag)) break;
-                    if (!sm100::mbar_wait(&full[s], (i / STAGES) & 1, abort_flag)) break;
-                    sm100::tc_fence_after();
-                    const uint64_t bdesc = sm100::sdesc_sw128(sm100::smem_u32(sB + (size_t)s * TILE_BYTES));
-#pragma unroll
-                    for (int k = 0; k < KP / 16; ++k)
-                        sm100::mma_f16(tmem + b * BN, adesc + 2 * k, bdesc + 2 * k, idesc, k > 0 ? 1u : 0u);
-                    sm100::mma_commit(&empty[s]);
-                    sm100::mma_commit(&acc_full[b]);
-                }
-            }
-            // every MMA has completed before TMEM is released
-            sm100::mma_commit(mma_done);
-            sm100::mbar_wait(mma_done, 0, abort_flag);
+            if (nslot == 1) issue<1>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            else if (nslot == 2) issue<2>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            else issue<4>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue: one (query, 32-column part) per thread ----------------
-        const int ew = warp - 2;                      // 0..15
-        const int quarter = warp & 3;                 // TMEM lane quarter this warp may access
-        const int part = ew >> 2;                     // which 32 columns of every tile
-        const int row = quarter * 32 + lane;
-        const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + part * PART;
-        bool ok = true;
-        int i = 0;
-        // pass 1: per-column minima of this part
-        float bm[PART];
-#pragma unroll
-        for (int c = 0; c < PART; ++c) bm[c] = __int_as_float(0x7f800000);
-        for (int r = r0; r < r1 && ok; ++r) {
-            const int rn = __ldg(p.rn + r);
-            for (int t = 0; t < rn; t += BN, ++i) {
-                const int b = i & 1;
-                if (!(ok = sm100::mbar_wait(&acc_full[b], (i >> 1) & 1, abort_flag))) break;
-                sm100::tc_fence_after();
-                const int lim = min(BN, rn - t) - part * PART;    // valid columns in this part
-                if (lim > 0) {
-                    float v[32];
-                    sm100::tmem_ld32(tbase + b * BN, v);
-                    if (lim >= 32) {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) bm[j] = fminf(bm[j], v[j]);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j)
-                            if (j < lim) bm[j] = fminf(bm[j], v[j]);
-                    }
-                }
-                sm100::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
-            }
-        }
-        // threshold: 64th smallest of the 128 column minima of every query
-        {
-            float *brow = reinterpret_cast<float *>(lists) + (size_t)row * BROW + part * PART;
-#pragma unroll
-            for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
-            epi_barrier();
-            for (int L = 0; L < 32 / PARTS; ++L) {
-                const int rowL = quarter * 32 + part * (32 / PARTS) + L;
-                const float *bl = reinterpret_cast<const float *>(lists) + (size_t)rowL * BROW;
-                unsigned v4[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) v4[u] = __float_as_uint(bl[u * 32 + lane]);
-                warp_bitonic<unsigned, 4>(v4, lane);
-                const unsigned kth = __shfl_sync(0xffffffffu, v4[63 % 4], 63 / 4);
-                if (lane == 0) sTau[rowL] = __uint_as_float(kth);
-            }
-            epi_barrier();              // minima rows are read; the list area may be reused
-        }
-        const float tau = sTau[row];
-        // pass 2: collect the candidates at or below tau
-        uint32_t *lrow = lists + ((size_t)row * PARTS + part) * LROWP;
-        int cnt = 0;
-        bool ovf = false;
-        for (int r = r0; r < r1 && ok; ++r) {
-            const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
-            for (int t = 0; t < rn; t += BN, ++i) {
-                const int b = i & 1;
-                if (!(ok = sm100::mbar_wait(&acc_full[b], (i >> 1) & 1, abort_flag))) break;
-                sm100::tc_fence_after();
-                const int lim = min(BN, rn - t) - part * PART;
-                if (lim > 0) {
-                    float v[32];
-                    sm100::tmem_ld32(tbase + b * BN, v);
-                    unsigned m = 0;
-#pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if (v[j] <= tau) m |= 1u << j;
-                    if (lim < 32) m &= (1u << lim) - 1u;
-                    if (cnt + __popc(m) > CAPP) { ovf = true; m = 0; }
-                    const uint32_t c0 = (uint32_t)(rs + t + part * PART);
-                    while (m) {
-                        const int j = __ffs(m) - 1;
-                        m &= m - 1u;
-                        lrow[cnt++] = c0 + (uint32_t)j;
-                    }
-                }
-                sm100::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
-            }
-        }
-        sCnt[row * PARTS + part] = ovf ? -1 : cnt;
-        epi_barrier();
-        // exact re-rank: this warp serves 8 of its quarter's queries
-        unsigned long long *ws = wkeys + (size_t)ew * WARP_KEYS;
-        for (int L = 0; L < 32 / PARTS && ok; ++L) {
-            const int rowL = quarter * 32 + part * (32 / PARTS) + L;
-            if (rowL >= nq) break;
-            const int q = qs + rowL;
-            int c[PARTS];
-            bool over = false, big = false;
-#pragma unroll
-            for (int u = 0; u < PARTS; ++u) { c[u] = sCnt[rowL * PARTS + u]; over |= c[u] < 0; }
-            if (over) {                               // finished by the exact fallback kernel
-                if (lane == 0) {
-                    const int k = atomicAdd(scratch + 0, 1);
-                    scratch[irc::kScratchLists + k] = q;
-                }
-                continue;
-            }
-            const int cL = c[0] + c[1] + c[2] + c[3];
-            big = cL > 128;
-            const uint32_t *lr = lists + (size_t)rowL * PARTS * LROWP;
-            const size_t o = (size_t)(q - p.q_base);
-            if (cL <= 64)
-                rerank<2>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
-            else if (!big)
-                rerank<4>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
-            else
-                rerank<8>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
-        }
+        epilogue(p, it, nt, qps, bps, tmem, lists, wkeys, sTau, sCnt, acc_full, acc_empty, abort_flag, F, nC, knn,
+                 vrKnn, rho, miKnn, d2Knn, scratch, warp, lane);
     }
     sm100::tc_fence_before();
     __syncthreads();
@@ -418,9 +553,8 @@ int launch_knn_bf16(const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, 
 {
     cudaError_t e = cudaFuncSetAttribute(k_knn_tc_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(BF16): smem attribute");
-    const int tiles = pl->ntiles[irc::tile_slot(BM)];
-    k_knn_tc_bf16<<<tiles, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, F, nC, knn, vrKnn, rho, miKnn, d2Knn,
-                                                     pl->scratch);
+    k_knn_tc_bf16<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, F, nC, knn, vrKnn, rho,
+                                                              miKnn, d2Knn, pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(BF16)");
     return IRC_OK;
 }

@@ -78,14 +78,14 @@ EncodeTiledFn encode_fn()
     return fn;
 }
 
-// Tensor map over a [rows x 64] BF16 matrix, 128-row boxes, 128-byte swizzle.
-int make_map(CUtensorMap *m, void *base, int rows)
+// Tensor map over a [rows x 64] BF16 matrix, box_rows-row boxes, 128-byte swizzle.
+int make_map(CUtensorMap *m, void *base, int rows, int box_rows)
 {
     EncodeTiledFn enc = encode_fn();
     if (!enc) { irc_host::set_error("cuTensorMapEncodeTiled unavailable"); return IRC_E_CUDA; }
     cuuint64_t dims[2] = {(cuuint64_t)irc_tc::KP, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)irc_tc::KP * 2};
-    cuuint32_t box[2] = {(cuuint32_t)irc_tc::KP, (cuuint32_t)irc_tc::BN};
+    cuuint32_t box[2] = {(cuuint32_t)irc_tc::KP, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -120,8 +120,8 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, (uint4 *)fq, (uint4 *)fc);
     IRC_CHECK_LAUNCH("irc_site_knn(BF16) prep");
     CUtensorMap mq, mc;
-    if ((rc = make_map(&mq, fq, nF)) != IRC_OK) return rc;
-    if ((rc = make_map(&mc, fc, nF)) != IRC_OK) return rc;
+    if ((rc = make_map(&mq, fq, nF, 32)) != IRC_OK) return rc;       // 32 query rows per lane quarter
+    if ((rc = make_map(&mc, fc, nF, irc_tc::BN)) != IRC_OK) return rc;
     rc = irc_tc::launch_knn_bf16(mq, mc, pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
     if (rc != IRC_OK) return rc;
     return irc_exact_overflow_drain(pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);

@@ -187,24 +187,20 @@ def build_plan(viDrift_out, vl_in, mlDrift):
     viiBB = np.concatenate([[0], change, [vd.size]]).astype(np.int64)
     viBB = vd[viiBB[:-1]]
     vnBB = np.diff(viiBB)
-    q0, nq, roff, rs, rn = [], [], [0], [], []
-    for a in range(int(vd_in.min()), int(vd_in.max()) + 1):
-        vii = np.flatnonzero(vd_in == a)
-        if vii.size == 0:
-            continue
-        lo, hi = int(vii[0]) + in_offset, int(vii[-1]) + in_offset
-        if hi - lo + 1 != vii.size:
-            raise ValueError("build_plan: chunk %d queries are not contiguous" % a)
-        linked = np.flatnonzero(ml[:, a])
-        runs = np.flatnonzero(np.isin(viBB, linked))
-        q0.append(lo)
-        nq.append(hi - lo + 1)
-        rs.extend(viiBB[runs].tolist())
-        rn.extend(vnBB[runs].tolist())
-        roff.append(len(rs))
+    # query chunks present in the in-set, in increasing chunk id
+    chunks, first, count = np.unique(vd_in, return_index=True, return_counts=True)
+    last = np.unique(vd_in[::-1], return_index=True)[1]
+    last = vd_in.size - 1 - last
+    if np.any(last - first + 1 != count):
+        bad = int(chunks[np.flatnonzero(last - first + 1 != count)[0]])
+        raise ValueError("build_plan: chunk %d queries are not contiguous" % bad)
+    # runs linked to every query chunk, in run order (ml[:, a] of each run's chunk)
+    link = ml[np.ix_(viBB, chunks)].T                      # [n query chunks x n runs]
+    a_idx, r_idx = np.nonzero(link)
+    roff = np.concatenate([[0], np.cumsum(np.bincount(a_idx, minlength=chunks.size))])
     i32 = lambda v: np.asarray(v, np.int32)
-    return dict(q0=i32(q0), nq=i32(nq), roff=i32(roff), rs=i32(rs), rn=i32(rn),
-                q_base=in_offset, n_out=int(vl.sum()), n_f=int(vd.size))
+    return dict(q0=i32(first + in_offset), nq=i32(count), roff=i32(roff), rs=i32(viiBB[r_idx]),
+                rn=i32(vnBB[r_idx]), q_base=in_offset, n_out=int(vl.sum()), n_f=int(vd.size))
 
 
 def plan_pairs(plan):

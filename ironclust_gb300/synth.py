@@ -21,7 +21,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .drift import build_plan, chunk_limits, dist_mask_ml, drift_mask
+from .drift import build_plan, chunk_limits, drift_mask
 
 
 def make_site(n_spk, n_dim, n_clusters, n_chunks, seed, drift_sd=0.3, drift_slope=0.0,
@@ -45,16 +45,31 @@ def make_site(n_spk, n_dim, n_clusters, n_chunks, seed, drift_sd=0.3, drift_slop
         ii = rng.choice(n_spk, size=n_noise, replace=False)
         F[ii] = rng.uniform(lo, hi, (n_noise, n_dim))
         lab[ii] = -1
-    # chunk similarity: -L2 distance between per-chunk centre snapshots
-    snap = (centres[None, :, :] + offs[:, None, :]).reshape(n_chunks, -1).T
+    # chunk similarity: -L2 distance between per-chunk centre snapshots (the
+    # centres move rigidly, so it is sqrt(K) times the distance of the offsets)
     if n_chunks == 1:
         ml = np.ones((1, 1), bool)
     else:
-        ml = dist_mask_ml(snap, drift_mask(n_chunks, band) if n_chunks > 2 * band + 1 else
-                          np.abs(np.arange(n_chunks)[None] - np.arange(n_chunks)[:, None]) <= band,
-                          min(n_link, n_chunks))
+        mask = (drift_mask(n_chunks, band) if n_chunks > 2 * band + 1 else
+                np.abs(np.arange(n_chunks)[None] - np.arange(n_chunks)[:, None]) <= band)
+        ml = link_chunks(offs, mask, min(n_link, n_chunks))
     return dict(F=F.astype(np.float32), viDrift=chunk.astype(np.int32), viLim=lim, mlDrift=ml,
                 labels=lab.astype(np.int32), n_dim=n_dim)
+
+
+def link_chunks(offs, mask, n_link):
+    """Column j = the n_link chunks nearest chunk j among the masked ones
+    (the set dist_mask_ml_ selects; a tie at the n_link-th distance has
+    probability zero for a continuous random walk).  Squared distances from
+    the Gram matrix, set selection by partition."""
+    sq = (offs * offs).sum(1)
+    d = sq[:, None] + sq[None, :] - 2.0 * offs @ offs.T
+    np.fill_diagonal(d, -1.0)                           # self first, exactly
+    d = np.where(mask, d, np.inf)
+    mi = np.argpartition(d, n_link - 1, axis=0)[:n_link]
+    ml = np.zeros(mask.shape, bool)
+    ml[mi, np.arange(mask.shape[1])[None, :]] = True
+    return ml
 
 
 def site_plan(site):
@@ -92,3 +107,11 @@ def probe_site_specs(n_sites=384, total=10_000_000, seed=1003, n_chunks=1200):
     ncl = rng.integers(12, 41, size=n_sites)
     return [dict(n_spk=int(n[i]), n_dim=int(dims[i]), n_clusters=int(ncl[i]),
                  n_chunks=n_chunks, seed=seed * 1000 + i) for i in range(n_sites)]
+
+
+def make_probe(n_sites=384, total=10_000_000, seed=1003, n_chunks=1200):
+    """The probe-scale batch: n_sites sites (lognormal spike counts, D in
+    {18, 24, 33}, 12-40 clusters) sharing n_chunks drift chunks."""
+    from .batch import SiteBatch
+    specs = probe_site_specs(n_sites, total, seed, n_chunks)
+    return SiteBatch(make_site(**s) for s in specs), specs
