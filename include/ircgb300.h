@@ -95,6 +95,14 @@ int irc_cuda_delta_knn(float *D, uint32_t *N, const float *B, const float *A,
 int irc_rho_drift(float *vrRho1, const int32_t *miSite12, const float *mrFet1,
                   const float *mrFet2, const int32_t *vnConst, float dc2, void *stream);
 
+/* Replaces jrc3_cuda_delta_drift (matlab/irc_cuda_delta_drift.cu:28; launched
+ * from matlab/irc.m:24663).  vnConst (host) = {n1, n12, nC}; vrRho1: [n12].
+ * vrDelta1 [n1] = sqrt(min d2 / dc2) over site-matched candidates with
+ * strictly higher rho; viNneigh1 [n1] 1-based (the query itself when none). */
+int irc_delta_drift(float *vrDelta1, uint32_t *viNneigh1, const int32_t *miSite12, const float *mrFet1,
+                    const float *mrFet2, const float *vrRho1, const int32_t *vnConst, float dc2,
+                    void *stream);
+
 /* ---------------------------------------------------------------------------
  * Fused per-site path.  A plan describes every launch the MATLAB chunk loop
  * of search_knn_drift_ / search_delta_drift_ (matlab/irc2.m:3764-3788,

@@ -34,6 +34,7 @@ SIGNATURES = {
     "irc_cuda_knn_index": [_P, _P, _P, _P, _P, _I, _P],
     "irc_cuda_delta_knn": [_P, _P, _P, _P, _P, _P, _P, _I, _P],
     "irc_rho_drift": [_P, _P, _P, _P, _P, _F, _P],
+    "irc_delta_drift": [_P, _P, _P, _P, _P, _P, _P, _F, _P],
     "irc_plan_create": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I],
     "irc_plan_destroy": [_P],
     "irc_plan_check": [_P, _P],

@@ -236,6 +236,73 @@ k_rho_drift(float *__restrict__ rho, const int *__restrict__ site12, const float
         rho[a0 + threadIdx.x] = (float)((double)sRho[threadIdx.x] / (double)sComp[threadIdx.x]);
 }
 
+// jrc3_cuda_delta_drift: nearest site-matched candidate with strictly higher
+// rho.  Thread t keeps its first strict minimum over j = t, t+128, ...; the
+// lowest thread holding the overall minimum wins; none -> the query itself.
+__global__ void __launch_bounds__(128)
+k_delta_drift(float *__restrict__ delta, unsigned *__restrict__ nneigh, const int *__restrict__ site12,
+              const float *__restrict__ f1, const float *__restrict__ f2, const float *__restrict__ rho, int n1,
+              int n12, int nC, float dc2)
+{
+    __shared__ __align__(16) float sA[IRC_NC_MAX * kQB];
+    __shared__ int sSite[kQB];
+    __shared__ float sR[kQB];
+    __shared__ unsigned long long sKey[kQB][128 / 32];
+    __shared__ unsigned sIdx[kQB][128 / 32];
+    const int a0 = blockIdx.x * kQB;
+    const int n = min(kQB, n1 - a0);
+    irc::stage_queries<kQB>(f1, nC, a0, n, sA);
+    if (threadIdx.x < kQB) {
+        sSite[threadIdx.x] = threadIdx.x < n ? __ldg(site12 + a0 + threadIdx.x) : INT_MIN;
+        sR[threadIdx.x] = __ldg(rho + a0 + min((int)threadIdx.x, n - 1));
+    }
+    __syncthreads();
+    float mn[kQB];
+    unsigned mi[kQB];
+#pragma unroll
+    for (int q = 0; q < kQB; ++q) { mn[q] = IRC_SINGLE_INF_F; mi[q] = 0u; }
+    for (int j = threadIdx.x; j < n12; j += blockDim.x) {
+        const float rj = __ldg(rho + j);
+        const int s1 = __ldg(site12 + j), s2 = __ldg(site12 + j + n12);
+#pragma unroll
+        for (int q = 0; q < kQB; ++q) {
+            if (rj <= sR[q]) continue;
+            const float *src = (s1 == sSite[q]) ? f1 : (s2 == sSite[q]) ? f2 : nullptr;
+            if (!src) continue;
+            src += (size_t)j * nC;
+            float acc = 0.0f;
+            for (int c = 0; c < nC; ++c) acc = irc::dterm(acc, sA[c * kQB + q], __ldg(src + c));
+            if (acc < mn[q]) { mn[q] = acc; mi[q] = (unsigned)j; }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kQB; ++q) {
+        unsigned long long k = irc::sort_key(mn[q], threadIdx.x);
+        unsigned idx = mi[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, o);
+            const unsigned oi = __shfl_xor_sync(0xffffffffu, idx, o);
+            if (ok < k) { k = ok; idx = oi; }
+        }
+        if (lane == 0) { sKey[q][warp] = k; sIdx[q][warp] = idx; }
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        const int q = threadIdx.x;
+        unsigned long long k = sKey[q][0];
+        unsigned idx = sIdx[q][0];
+        for (int w = 1; w < 4; ++w)
+            if (sKey[q][w] < k) { k = sKey[q][w]; idx = sIdx[q][w]; }
+        const float v = __uint_as_float((unsigned)(k >> 32));
+        const bool found = v < IRC_SINGLE_INF_F;
+        const float dmin = found ? v : IRC_SINGLE_INF_F;
+        delta[a0 + q] = __fsqrt_rn(__fdiv_rn(fabsf(dmin), dc2));
+        nneigh[a0 + q] = (found ? idx : (unsigned)(a0 + q)) + 1u;
+    }
+}
+
 inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 }  // namespace
@@ -243,7 +310,7 @@ inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 // Exact top-k fill of the search_min_drift output (IRC_MODE_EXACT), in irc_site.cu.
 int irc_exact_chunk_fill(float *D, int32_t *I, const float *F, const int32_t *IBB,
                          const int32_t *NBB, int nC, int nBB, int iA0, int nA, int nT, int knn,
-                         cudaStream_t s);
+                         int nF, cudaStream_t s);
 
 extern "C" {
 
@@ -265,7 +332,7 @@ int irc_search_min_drift(float *D, int32_t *I, const float *F, const int32_t *IB
     cudaStream_t s = (cudaStream_t)stream;
     if (mode == IRC_MODE_EXACT) {
         if (knn <= 0 || knn > nThreads) { irc_host::set_error("irc_search_min_drift: bad knn %d", knn); return IRC_E_INVAL; }
-        return irc_exact_chunk_fill(D, I, F, IBB, NBB, nC, nBB, iA0, nA, nThreads, knn, s);
+        return irc_exact_chunk_fill(D, I, F, IBB, NBB, nC, nBB, iA0, nA, nThreads, knn, vnConst[1], s);
     }
     if (mode != IRC_MODE_REF) { irc_host::set_error("irc_search_min_drift: unsupported mode %d", mode); return IRC_E_UNSUPPORTED; }
     k_search_drift<false><<<cdiv(nA, kQB), kThreads, 0, s>>>(D, I, F, nullptr, IBB, NBB, nC, nBB, iA0, nA, nThreads);
@@ -335,6 +402,22 @@ int irc_rho_drift(float *vrRho1, const int32_t *miSite12, const float *mrFet1, c
     if (nC <= 0 || n1 <= 0 || n12 < n1) { irc_host::set_error("irc_rho_drift: bad sizes n1=%d n12=%d nC=%d", n1, n12, nC); return IRC_E_INVAL; }
     k_rho_drift<<<cdiv(n1, kQB), 128, 0, (cudaStream_t)stream>>>(vrRho1, miSite12, mrFet1, mrFet2, n1, n12, nC, dc2);
     IRC_CHECK_LAUNCH("irc_rho_drift");
+    return IRC_OK;
+}
+
+int irc_delta_drift(float *vrDelta1, uint32_t *viNneigh1, const int32_t *miSite12, const float *mrFet1,
+                    const float *mrFet2, const float *vrRho1, const int32_t *vnConst, float dc2, void *stream)
+{
+    if (!vrDelta1 || !viNneigh1 || !miSite12 || !mrFet1 || !mrFet2 || !vrRho1 || !vnConst) {
+        irc_host::set_error("irc_delta_drift: null pointer");
+        return IRC_E_INVAL;
+    }
+    const int n1 = vnConst[0], n12 = vnConst[1], nC = vnConst[2];
+    if (nC > IRC_NC_MAX) { irc_host::set_error("irc_delta_drift: nC=%d > %d", nC, IRC_NC_MAX); return IRC_E_NC; }
+    if (nC <= 0 || n1 <= 0 || n12 < n1) { irc_host::set_error("irc_delta_drift: bad sizes n1=%d n12=%d nC=%d", n1, n12, nC); return IRC_E_INVAL; }
+    k_delta_drift<<<cdiv(n1, kQB), 128, 0, (cudaStream_t)stream>>>(vrDelta1, viNneigh1, miSite12, mrFet1, mrFet2,
+                                                                  vrRho1, n1, n12, nC, dc2);
+    IRC_CHECK_LAUNCH("irc_delta_drift");
     return IRC_OK;
 }
 

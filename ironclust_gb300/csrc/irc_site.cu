@@ -225,11 +225,66 @@ int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, size_t row_bytes)
     return IRC_OK;
 }
 
-int irc_exact_chunk_fill(float *, int32_t *, const float *, const int32_t *, const int32_t *, int,
-                         int, int, int, int, int, cudaStream_t)
+namespace {
+
+// [nT x nA] search_min_drift output holding the exact kNN in rows 0..knn-1
+// (ascending) and the no-candidate sentinel in the others, so the unchanged
+// MATLAB post-processing (stable sort, first knn rows) returns the exact kNN.
+__global__ void k_expand_exact(float *__restrict__ D, int *__restrict__ I, const int *__restrict__ miKnn,
+                               const float *__restrict__ d2Knn, int nA, int nT, int knn, int iA0)
 {
-    irc_host::set_error("irc_search_min_drift: IRC_MODE_EXACT is served by irc_site_knn");
-    return IRC_E_UNSUPPORTED;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)nA * nT) return;
+    const int a = (int)(i / nT), t = (int)(i % nT);
+    if (t < knn) {
+        D[i] = irc::ref_sqrt_abs(d2Knn[(size_t)a * knn + t]);
+        I[i] = miKnn[(size_t)a * knn + t];
+    } else {
+        D[i] = irc::ref_sqrt_abs(IRC_SINGLE_INF_F);
+        I[i] = iA0 + a + 1;
+    }
+}
+
+}  // namespace
+
+// IRC_MODE_EXACT of the search_min_drift drop-in: a one-chunk plan through the
+// EXACT site kernel, then the expansion above.  The drop-in receives IBB/NBB
+// on the device, so they are read back first; the plan and the temporaries
+// are created and released per call (stream-ordered allocation).
+int irc_exact_chunk_fill(float *D, int32_t *I, const float *F, const int32_t *IBB, const int32_t *NBB, int nC,
+                         int nBB, int iA0, int nA, int nT, int knn, int nF, cudaStream_t s)
+{
+    std::vector<int32_t> rs(nBB), rn(nBB);
+    cudaError_t e = cudaMemcpyAsync(rs.data(), IBB, 4 * (size_t)nBB, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rn.data(), NBB, 4 * (size_t)nBB, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_search_min_drift(EXACT): read IBB/NBB");
+    const int32_t q0[1] = {iA0}, nq[1] = {nA}, roff[2] = {0, nBB};
+    irc_plan *pl = nullptr;
+    int rc = irc_plan_create(&pl, q0, nq, roff, rs.data(), rn.data(), 1, iA0, nA, nF);
+    if (rc != IRC_OK) return rc;
+    float *vr = nullptr, *d2 = nullptr;
+    int32_t *mi = nullptr;
+    e = cudaMallocAsync(&vr, sizeof(float) * (size_t)nA, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d2, sizeof(float) * (size_t)nA * knn, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&mi, sizeof(int32_t) * (size_t)nA * knn, s);
+    if (e == cudaSuccess) {
+        rc = irc_site_knn(pl, F, nC, knn, nT, IRC_MODE_EXACT, vr, nullptr, mi, d2, s);
+        if (rc == IRC_OK) {
+            const size_t n = (size_t)nA * nT;
+            k_expand_exact<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(D, I, mi, d2, nA, nT, knn, iA0);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) rc = irc_host::cuda_status(e, "irc_search_min_drift(EXACT): expand");
+        }
+    } else {
+        rc = irc_host::cuda_status(e, "irc_search_min_drift(EXACT): temporaries");
+    }
+    if (vr) cudaFreeAsync(vr, s);
+    if (d2) cudaFreeAsync(d2, s);
+    if (mi) cudaFreeAsync(mi, s);
+    cudaStreamSynchronize(s);                    // the plan's image is released with the call
+    irc_plan_destroy(pl);
+    return rc;
 }
 
 // Exact / tensor-core site kernels (irc_exact.cu, irc_tc.cu).

@@ -124,6 +124,18 @@ def rho_drift(miSite12_colmajor, mrFet1, mrFet2, n1, dc2):
     return rho
 
 
+def delta_drift(miSite12_colmajor, mrFet1, mrFet2, vrRho12, n1, dc2):
+    """feval(jrc3_cuda_delta_drift, vrDelta1, viNneigh1, miSite12, mrFet1, mrFet2, vrRho1, vnConst, dc2).
+    Returns delta [n1] and nneigh [n1] (1-based, uint32 bits in int32)."""
+    n12, nC = mrFet1.shape
+    vn = _i32host([n1, n12, nC])
+    de = torch.empty(n1, dtype=torch.float32, device=mrFet1.device)
+    nn = torch.empty(n1, dtype=torch.int32, device=mrFet1.device)
+    check(lib().irc_delta_drift(_p(de), _p(nn), _p(miSite12_colmajor), _p(mrFet1), _p(mrFet2), _p(vrRho12),
+                                vn.ctypes.data_as(C.c_void_p), C.c_float(dc2), _stream()), "irc_delta_drift")
+    return de, nn
+
+
 # ---------------------------------------------------------------------------
 # MATLAB post-processing on the device
 # ---------------------------------------------------------------------------
@@ -328,6 +340,17 @@ def cuda_delta_knn_host(mrFet, vrRho, vi2, vi1):
     D, N = cuda_delta_knn(mrFet[vi2].contiguous(), mrFet[vi1].contiguous(),
                           vrRho[vi2].contiguous(), vrRho[vi1].contiguous())
     return D, vi2[N.long() - 1]
+
+
+def cuda_delta_drift(viSite1, viSite2, mrFet1, mrFet2, vrRho12, n1, dc2):
+    """cuda_delta_drift_ (matlab/irc.m:24641-24666) for one drift window of
+    n12 spikes (own chunk first): delta = sqrt(min d2 / dc2) and nneigh
+    (1-based into the window)."""
+    site = torch.cat([torch.as_tensor(viSite1, dtype=torch.int32),
+                      torch.as_tensor(viSite2, dtype=torch.int32)]).to(mrFet1.device)
+    return delta_drift(site, mrFet1.contiguous(), mrFet2.contiguous(),
+                       torch.as_tensor(vrRho12, dtype=torch.float32, device=mrFet1.device).contiguous(),
+                       n1, float(np.float32(dc2)))
 
 
 def cuda_rho_drift(viSite1, viSite2, mrFet1, mrFet2, n1, dc2):

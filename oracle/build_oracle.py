@@ -25,7 +25,7 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 REFERENCE_MATLAB = "/root/reference/matlab"
 REF_KERNELS = ["search_min_drift", "search_delta_drift", "cuda_knn_index",
-               "cuda_delta_knn", "irc_cuda_rho_drift"]
+               "cuda_delta_knn", "irc_cuda_rho_drift", "irc_cuda_delta_drift"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
 

@@ -571,3 +571,43 @@ void orc_exact_delta_f32(int32_t *nn, float *d2out, const float *F, const float 
         }
     }
 }
+
+/* irc_cuda_delta_drift.cu:28-131 (jrc3_cuda_delta_drift).  vnConst = {n1,
+ * n12, nC}.  For query i1 (site s = site1[i1], rho R[i1]) the candidates j
+ * of the n12 window with R[j] > R[i1] (masked when R[j] <= R[i1]) and a site
+ * match (primary features when site1[j] == s, else secondary when
+ * site2[j] == s); distance query minus candidate, fused per feature; each
+ * of the nT = 128 threads keeps its first strict minimum over j = t, t+nT,
+ * ...; the lowest thread holding the overall minimum wins; no candidate ->
+ * SINGLE_INF and the query itself.  delta = sqrt(min / dc2) (the source's
+ * ABS applies to a non-negative value), nneigh = index + 1. */
+void orc_delta_drift(float *vrDelta1, uint32_t *viNneigh1, const int32_t *miSite12, const float *mrFet1,
+                     const float *mrFet2, const float *vrRho1, const int32_t *vnConst, float dc2)
+{
+    const int n1 = vnConst[0], n12 = vnConst[1], nC = vnConst[2], nT = 128;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i1 = 0; i1 < n1; ++i1) {
+        const int s = miSite12[i1];
+        const float *q = mrFet1 + (size_t)i1 * nC;
+        const float rq = vrRho1[i1];
+        float best = ORC_SINGLE_INF;
+        uint32_t bi = (uint32_t)i1;
+        for (int t = 0; t < nT; ++t) {
+            float tmin = ORC_SINGLE_INF;
+            uint32_t timin = (uint32_t)i1;
+            for (int j = t; j < n12; j += nT) {
+                if (vrRho1[j] <= rq) continue;
+                const float *c;
+                if (miSite12[j] == s) c = mrFet1 + (size_t)j * nC;
+                else if (miSite12[j + n12] == s) c = mrFet2 + (size_t)j * nC;
+                else continue;
+                float acc = 0.0f;
+                for (int k = 0; k < nC; ++k) { float d = q[k] - c[k]; acc = fmaf(d, d, acc); }
+                if (acc < tmin) { tmin = acc; timin = (uint32_t)j; }
+            }
+            if (tmin < best) { best = tmin; bi = timin; }
+        }
+        vrDelta1[i1] = sqrtf((best < 0 ? -best : best) / dc2);
+        viNneigh1[i1] = bi + 1;
+    }
+}

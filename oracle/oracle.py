@@ -40,7 +40,7 @@ def lib():
                      "orc_cuda_delta_knn", "orc_rho_drift", "orc_post_sort_knn", "orc_post_min",
                      "orc_exact_knn_f64", "orc_exact_delta_f64", "orc_knn_cpu", "orc_delta_cpu",
                      "orc_site_knn_cpu", "orc_site_delta_cpu", "orc_exact_knn_f32",
-                     "orc_exact_delta_f32"):
+                     "orc_exact_delta_f32", "orc_delta_drift"):
             getattr(_lib, name).restype = None
     return _lib
 
@@ -114,6 +114,19 @@ def rho_drift(miSite12, mrFet1, mrFet2, n1, dc2):
     rho = np.empty(n1, np.float32)
     lib().orc_rho_drift(_ptr(rho), _ptr(site), _ptr(f1), _ptr(f2), _ptr(vn), C.c_float(dc2))
     return rho
+
+
+def delta_drift(miSite12, mrFet1, mrFet2, rho, n1, dc2):
+    """jrc3_cuda_delta_drift restated; rho: [n12]."""
+    f1, f2 = _fet(mrFet1), _fet(mrFet2)
+    n12, nC = f1.shape
+    site = _i32(np.asarray(miSite12).T)
+    vn = _i32([n1, n12, nC])
+    de = np.empty(n1, np.float32)
+    nn = np.empty(n1, np.uint32)
+    lib().orc_delta_drift(_ptr(de), _ptr(nn), _ptr(site), _ptr(f1), _ptr(f2), _ptr(_f32(rho)), _ptr(vn),
+                          C.c_float(dc2))
+    return de, nn
 
 
 # --- MATLAB post-processing ----------------------------------------------------
@@ -293,6 +306,17 @@ class RefKernels:
                                                self._p(R_B), self._p(R_A), self._p(vn),
                                                C.c_int(nA), self._s()))
         return D, N
+
+    def delta_drift(self, miSite12_colmajor, mrFet1, mrFet2, rho, n1, dc2):
+        t = self.torch
+        n12, nC = mrFet1.shape
+        vn = t.tensor([n1, n12, nC], dtype=t.int32, device=mrFet1.device)
+        de = t.zeros(n1, dtype=t.float32, device=mrFet1.device)
+        nn = t.zeros(n1, dtype=t.int32, device=mrFet1.device)
+        self._check(self.h.refh_delta_drift(self._p(de), self._p(nn), self._p(miSite12_colmajor), self._p(mrFet1),
+                                            self._p(mrFet2), self._p(rho), self._p(vn), C.c_float(dc2),
+                                            C.c_int(n1), self._s()))
+        return de, nn
 
     def rho_drift(self, miSite12_colmajor, mrFet1, mrFet2, n1, dc2):
         t = self.torch

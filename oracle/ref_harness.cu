@@ -33,10 +33,10 @@
 
 namespace {
 
-enum { K_MIN = 0, K_DELTA, K_KNN, K_DKNN, K_RHO, K_COUNT };
+enum { K_MIN = 0, K_DELTA, K_KNN, K_DKNN, K_RHO, K_DDRIFT, K_COUNT };
 const char *kFiles[K_COUNT] = {"search_min_drift.ptx", "search_delta_drift.ptx",
                                "cuda_knn_index.ptx", "cuda_delta_knn.ptx",
-                               "irc_cuda_rho_drift.ptx"};
+                               "irc_cuda_rho_drift.ptx", "irc_cuda_delta_drift.ptx"};
 cudaLibrary_t g_lib[K_COUNT];
 cudaKernel_t g_kern[K_COUNT];
 bool g_loaded = false;
@@ -130,6 +130,18 @@ int refh_rho_drift(float *vrRho1, const int *miSite12, const float *mrFet1, cons
     void *args[] = {&vrRho1, &miSite12, &mrFet1, &mrFet2, &vnConst_dev, &dc2};
     return (int)launch(K_RHO, dim3(cdiv(n1, CHUNK * CHUNK), CHUNK), dim3(nThreads),
                        4 * CHUNK * (nC_max + 1 + 2 * nThreads), (cudaStream_t)stream, args);
+}
+
+// jrc3_cuda_delta_drift: block 128, grid [ceil(n1/256), 16], smem 4*16*(45+2+2*128)
+// (matlab/irc.m:24646-24663)
+int refh_delta_drift(float *vrDelta1, unsigned *viNneigh1, const int *miSite12, const float *mrFet1,
+                     const float *mrFet2, const float *vrRho1, const int *vnConst_dev, float dc2, int n1,
+                     void *stream)
+{
+    const int CHUNK = 16, nC_max = 45, nThreads = 128;
+    void *args[] = {&vrDelta1, &viNneigh1, &miSite12, &mrFet1, &mrFet2, &vrRho1, &vnConst_dev, &dc2};
+    return (int)launch(K_DDRIFT, dim3(cdiv(n1, CHUNK * CHUNK), CHUNK), dim3(nThreads),
+                       4 * CHUNK * (nC_max + 2 + 2 * nThreads), (cudaStream_t)stream, args);
 }
 
 }  // extern "C"

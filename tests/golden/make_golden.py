@@ -77,6 +77,10 @@ def main(out):
     dc2 = np.float32(20.0)
     rho = rk.rho_drift(t(np.concatenate([s1, s2])), t(f1), t(f2), 200, float(dc2))
     g.update(rho_f1=f1, rho_f2=f2, rho_s1=s1, rho_s2=s2, rho_dc2=dc2, rho_out=rho.cpu().numpy())
+    # --- jrc3_cuda_delta_drift (rho of all 800 spikes of the window) ------------------
+    r12 = rho_with_ties(800, 26)
+    de, nn = rk.delta_drift(t(np.concatenate([s1, s2])), t(f1), t(f2), t(r12), 200, float(dc2))
+    g.update(ddrift_rho=r12, ddrift_delta=de.cpu().numpy(), ddrift_nn=nn.cpu().numpy())
     torch.cuda.synchronize()
     np.savez_compressed(out, **g)
     print("wrote", out, os.path.getsize(out), "bytes")

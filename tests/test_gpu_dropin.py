@@ -50,6 +50,26 @@ def test_search_min_drift_bitexact(gpu, refk, case, nT):
 
 
 @pytest.mark.parametrize("case", CASES)
+def test_search_min_drift_exact_mode(gpu, case):
+    """IRC_MODE_EXACT fills rows 0..knn-1 so that the unchanged MATLAB sort
+    returns the exact kNN of the chunk."""
+    F, plan, _ = small_site(**case)
+    Fd = torch.from_numpy(F).to(gpu)
+    idx, d2 = O.exact_knn_f32(F, plan, 30)
+    for i in range(len(plan["q0"])):
+        r0, r1 = plan["roff"][i], plan["roff"][i + 1]
+        IBB = torch.from_numpy(plan["rs"][r0:r1]).to(gpu)
+        NBB = torch.from_numpy(plan["rn"][r0:r1]).to(gpu)
+        q0, nq = int(plan["q0"][i]), int(plan["nq"][i])
+        D, I = irc.search_min_drift(Fd, IBB, NBB, [F.shape[1], F.shape[0], int(r1 - r0), q0, nq],
+                                    nThreads=1024, mode="exact", knn=30)
+        v, m = O.post_sort_knn(D.cpu().numpy(), I.cpu().numpy(), 30)
+        o = q0 - plan["q_base"]
+        assert np.array_equal(m, idx[o:o + nq]), i
+        assert np.array_equal(bits(v), bits(np.sqrt(d2[o:o + nq, 29]).astype(np.float32))), i
+
+
+@pytest.mark.parametrize("case", CASES)
 def test_search_delta_drift_bitexact(gpu, refk, case):
     F, plan, _ = small_site(**case)
     R = rho_with_ties(F.shape[0])
@@ -97,6 +117,26 @@ def test_cuda_delta_knn_bitexact(gpu, refk, nB, nA, nC):
     assert same(D, Dr) and same(N, Nr)
     Do, No = O.cuda_delta_knn(B, A, RB, RA)
     assert same(D, Do) and np.array_equal(N.cpu().numpy().view(np.uint32), No)
+
+
+@pytest.mark.parametrize("n12,n1,nC", [(1500, 300, 33), (700, 700, 24), (2000, 17, 45)])
+def test_delta_drift_bitexact(gpu, refk, n12, n1, nC):
+    rng = np.random.default_rng(n12 * 7 + n1)
+    f1 = rng.normal(0, 2, (n12, nC)).astype(np.float32)
+    f2 = (f1 + rng.normal(0, 0.5, (n12, nC))).astype(np.float32)
+    f1[3] = f1[2]                                             # a zero distance (kept by this kernel)
+    s1 = rng.integers(1, 4, n12).astype(np.int32)
+    s2 = rng.integers(1, 4, n12).astype(np.int32)
+    rho = rho_with_ties(n12, 9)
+    rho[0] = rho.max() + 1                                    # a query with no higher-rho candidate
+    dc2 = float(np.float32(17.5))
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(gpu)
+    site_cm = t(np.concatenate([s1, s2]))
+    de, nn = irc.delta_drift(site_cm, t(f1), t(f2), t(rho), n1, dc2)
+    dr, nr = refk.delta_drift(site_cm, t(f1), t(f2), t(rho), n1, dc2)
+    assert same(de, dr) and same(nn, nr)
+    do, no = O.delta_drift(np.stack([s1, s2], 1), f1, f2, rho, n1, dc2)
+    assert same(de, do) and np.array_equal(nn.cpu().numpy().view(np.uint32), no)
 
 
 @pytest.mark.parametrize("n12,n1,nC", [(1500, 300, 33), (700, 700, 24), (2000, 17, 45)])

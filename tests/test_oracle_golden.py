@@ -62,6 +62,15 @@ def test_rho_drift_restatement(g):
     assert np.array_equal(bits(rho), bits(g["rho_out"]))
 
 
+def test_delta_drift_restatement(g):
+    if "ddrift_delta" not in g:
+        pytest.skip("fixture predates the delta_drift case")
+    site = np.stack([g["rho_s1"], g["rho_s2"]], 1)
+    de, nn = O.delta_drift(site, g["rho_f1"], g["rho_f2"], g["ddrift_rho"], 200, float(g["rho_dc2"]))
+    assert np.array_equal(bits(de), bits(g["ddrift_delta"]))
+    assert np.array_equal(nn.view(np.int32), g["ddrift_nn"])
+
+
 def test_planted_mistake_is_caught(g):
     """A one-ulp change in one feature must change the restated output."""
     F = g["s1_F"].copy()
