@@ -223,7 +223,7 @@ def run_ours(args):
                 roof = {"bound": "fp32-simt", "kernel": dom_name, "achieved": ach, "peak": fp32_peak,
                         "unit": "TFLOP/s", "frac": ach / fp32_peak, "traffic": None,
                         "peak_src": "nominal 152 SM x 128 lanes x 2.07 GHz"}
-        n_launch = {"ref": 2, "exact": 5, "bf16": 6, "fp8": 6}
+        n_launch = {"ref": 2, "exact": 5, "bf16": 6, "fp8": 7}
         out = {
             "metric": METRIC, "value": hr.get("spikes_per_s"), "unit": "spikes/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": hr.get("ms_per_step"),
@@ -450,7 +450,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="bf16")
-    ap.add_argument("--forms", default="bf16,exact,ref")
+    ap.add_argument("--forms", default="bf16,fp8,exact,ref")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-chunks", type=int, default=4)
@@ -458,7 +458,7 @@ def main(argv=None):
     ap.add_argument("--batched", dest="batched", action="store_true", default=True,
                     help="also time the probe-scale batch (all sites in one plan, CUDA graph)")
     ap.add_argument("--no-batched", dest="batched", action="store_false")
-    ap.add_argument("--batched-forms", default="bf16,exact")
+    ap.add_argument("--batched-forms", default="bf16,fp8,exact,ref")
     ap.add_argument("--batched-steps", type=int, default=3)
     ap.add_argument("--probe-sites", type=int, default=384)
     ap.add_argument("--probe-spikes", type=int, default=10_000_000)

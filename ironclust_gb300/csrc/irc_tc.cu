@@ -430,13 +430,15 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
 
 // MMA issuer (one thread), in the producer's order; slot s's tile k goes to
 // accumulator s*BPS + k % BPS.
-template <int NS>
+template <int NS, bool FP8>
 __device__ __forceinline__ void issue(const int (&nt)[4], uint32_t tmem, uint8_t *sA, uint8_t *sB, uint64_t *full,
                                       uint64_t *empty, uint64_t *a_full, uint64_t *acc_full, uint64_t *acc_empty,
                                       uint64_t *mma_done, volatile int *abort_flag)
 {
     constexpr int BPS = NBUF / NS;
-    constexpr uint32_t idesc = sm100::idesc_make(BM, BN, 1, 1);   // bf16 x bf16 -> f32
+    // bf16 x bf16 (kind::f16, K = 16) or e4m3 x e4m3 (kind::f8f6f4, K = 32) -> f32;
+    // either way one MMA consumes 32 bytes of every 128-byte operand row
+    constexpr uint32_t idesc = FP8 ? sm100::idesc_make(BM, BN, 0, 0) : sm100::idesc_make(BM, BN, 1, 1);
     if (sm100::mbar_wait(a_full, 0, abort_flag)) {
         sm100::tc_fence_after();
         const uint64_t adesc = sm100::sdesc_sw128(sm100::smem_u32(sA));
@@ -459,7 +461,10 @@ __device__ __forceinline__ void issue(const int (&nt)[4], uint32_t tmem, uint8_t
                         const uint64_t bdesc = sm100::sdesc_sw128(sm100::smem_u32(sB + (size_t)st * TILE_BYTES));
 #pragma unroll
                         for (int kk = 0; kk < KP / 16; ++kk)
-                            sm100::mma_f16(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
+                            if (FP8)
+                                sm100::mma_f8(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
+                            else
+                                sm100::mma_f16(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
                         sm100::mma_commit(&empty[st]);
                         sm100::mma_commit(&acc_full[b]);
                         ++i;
@@ -474,8 +479,9 @@ __device__ __forceinline__ void issue(const int (&nt)[4], uint32_t tmem, uint8_t
     sm100::mbar_wait(mma_done, 0, abort_flag);
 }
 
+template <bool FP8>
 __global__ void __launch_bounds__(THREADS, 1)
-k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
+k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
               const irc_tc::TcItem *__restrict__ items, const float *__restrict__ F, int nC, int knn,
               float *__restrict__ vrKnn, float *__restrict__ rho, int *__restrict__ miKnn,
               float *__restrict__ d2Knn, int *__restrict__ scratch)
@@ -526,9 +532,9 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            if (nslot == 1) issue<1>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
-            else if (nslot == 2) issue<2>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
-            else issue<4>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            if (nslot == 1) issue<1, FP8>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            else if (nslot == 2) issue<2, FP8>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            else issue<4, FP8>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
         }
         __syncwarp();
     } else {
@@ -548,14 +554,15 @@ k_knn_tc_bf16(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ C
 
 namespace irc_tc {
 
-int launch_knn_bf16(const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F, int nC, int knn,
-                    float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, cudaStream_t s)
+int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F, int nC,
+                  int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, cudaStream_t s)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_knn_tc_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
-    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(BF16): smem attribute");
-    k_knn_tc_bf16<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, F, nC, knn, vrKnn, rho,
+    auto kern = fp8 ? k_knn_tc<true> : k_knn_tc<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): smem attribute");
+    kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, F, nC, knn, vrKnn, rho,
                                                               miKnn, d2Knn, pl->scratch);
-    IRC_CHECK_LAUNCH("irc_site_knn(BF16)");
+    IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
     return IRC_OK;
 }
 

@@ -10,6 +10,8 @@
 // features, accumulated in FP32.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 #include "irc_common.cuh"
 #include "irc_plan.cuh"
@@ -60,6 +62,87 @@ __global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, uint4 *
     }
 }
 
+// |F| maximum (bits of a non-negative float, so integer max == float max).
+__global__ void k_absmax(const float *__restrict__ F, size_t n, unsigned *__restrict__ out)
+{
+    unsigned m = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        m = max(m, __float_as_uint(fabsf(__ldg(F + i))));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__device__ __forceinline__ unsigned char to_e4m3(float x)
+{
+    return (unsigned char)__nv_cvt_float_to_fp8(x, __NV_SATFINITE, __NV_E4M3);
+}
+
+__device__ __forceinline__ float from_e4m3(unsigned char v)
+{
+    const __half_raw h = __nv_cvt_fp8_to_halfraw((__nv_fp8_storage_t)v, __NV_E4M3);
+    return __half2float(__half(h));
+}
+
+// FP8 rows of 128 e4m3 values (K = 128, 128 bytes).  With x = e4m3(s*a),
+// y = e4m3(s*b) and s = 32 / max|F| (so |x| <= 32 and -2x is exact):
+//     query row     [ -2x_1 .. -2x_D, nx_0 .. nx_5, 2^e_0 .. 2^e_5, 0 ... ]
+//     candidate row [    y_1 ..  y_D, 2^e_0 .. 2^e_5, ny_0 .. ny_5, 0 ... ]
+// where |x|^2 = sum_t nx_t * 2^e_t (e = 8, 4, 0, -4, -8, -9: each e4m3 piece
+// takes the next 4 bits of the remainder), so the contraction is
+// s^2 |a - b|^2 of the rounded features -- a positive multiple, which the
+// filter only compares.
+constexpr int kFp8Pieces = 6;
+__device__ __forceinline__ int piece_exp(int t) { return t < 5 ? 8 - 4 * t : -9; }
+
+__global__ void k_prep_fp8(const float *__restrict__ F, int nF, int nC, const unsigned *__restrict__ amax,
+                           uint4 *__restrict__ Fq, uint4 *__restrict__ Fc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nF) return;
+    const float am = __uint_as_float(*amax);
+    const float sc = am > 0.0f ? 32.0f / am : 1.0f;
+    const float *a = F + (size_t)i * nC;
+    float nx = 0.0f;
+    for (int k = 0; k < nC; ++k) {
+        const float x = from_e4m3(to_e4m3(sc * __ldg(a + k)));
+        nx = __fmaf_rn(x, x, nx);
+    }
+    unsigned char pc[kFp8Pieces], pf[kFp8Pieces];
+    float rem = nx;
+#pragma unroll
+    for (int t = 0; t < kFp8Pieces; ++t) {
+        const float f = ldexpf(1.0f, piece_exp(t));
+        pc[t] = to_e4m3(rem / f);
+        pf[t] = to_e4m3(f);
+        rem -= from_e4m3(pc[t]) * f;
+    }
+#pragma unroll 1
+    for (int j = 0; j < 128 / 16; ++j) {
+        __align__(16) unsigned char wq[16], wc[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            const int k = j * 16 + e;
+            unsigned char vq = 0, vc = 0;
+            if (k < nC) {
+                const unsigned char y = to_e4m3(sc * __ldg(a + k));
+                vc = y;
+                vq = to_e4m3(-2.0f * from_e4m3(y));
+            } else if (k < nC + kFp8Pieces) {
+                vq = pc[k - nC];
+                vc = pf[k - nC];
+            } else if (k < nC + 2 * kFp8Pieces) {
+                vq = pf[k - nC - kFp8Pieces];
+                vc = pc[k - nC - kFp8Pieces];
+            }
+            wq[e] = vq;
+            wc[e] = vc;
+        }
+        Fq[(size_t)i * 8 + j] = *reinterpret_cast<uint4 *>(wq);
+        Fc[(size_t)i * 8 + j] = *reinterpret_cast<uint4 *>(wc);
+    }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -78,16 +161,19 @@ EncodeTiledFn encode_fn()
     return fn;
 }
 
-// Tensor map over a [rows x 64] BF16 matrix, box_rows-row boxes, 128-byte swizzle.
-int make_map(CUtensorMap *m, void *base, int rows, int box_rows)
+// Tensor map over [rows x 128 bytes] operand rows (64 BF16 or 128 e4m3 values),
+// box_rows-row boxes, 128-byte swizzle.
+int make_map(CUtensorMap *m, void *base, int rows, int box_rows, bool fp8)
 {
     EncodeTiledFn enc = encode_fn();
     if (!enc) { irc_host::set_error("cuTensorMapEncodeTiled unavailable"); return IRC_E_CUDA; }
-    cuuint64_t dims[2] = {(cuuint64_t)irc_tc::KP, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)irc_tc::KP * 2};
-    cuuint32_t box[2] = {(cuuint32_t)irc_tc::KP, (cuuint32_t)box_rows};
+    const int inner = fp8 ? 128 : irc_tc::KP;
+    cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)128};
+    cuuint32_t box[2] = {(cuuint32_t)inner, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+    CUresult r = enc(m, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims,
+                     strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { irc_host::set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return IRC_E_CUDA; }
@@ -105,11 +191,11 @@ int irc_exact_overflow_drain(irc_plan *pl, const float *F, int nC, int knn, floa
 int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, float *vrKnn, float *rho,
                     int32_t *miKnn, float *d2Knn, cudaStream_t s)
 {
-    if (mode != IRC_MODE_BF16) {
-        irc_host::set_error("irc_site_knn: FP8 tensor-core mode not available");
-        return IRC_E_UNSUPPORTED;
+    const bool fp8 = mode == IRC_MODE_FP8;
+    if (nC + (fp8 ? 2 * kFp8Pieces : 6) > (fp8 ? 128 : irc_tc::KP)) {
+        irc_host::set_error("irc_site_knn(tensor core): nC=%d too large", nC);
+        return IRC_E_NC;
     }
-    if (nC + 6 > irc_tc::KP) { irc_host::set_error("irc_site_knn(BF16): nC=%d > %d", nC, irc_tc::KP - 6); return IRC_E_NC; }
     if (knn > irc_tc::KNN_MAX) { irc_host::set_error("irc_site_knn(BF16): knn %d > %d", knn, irc_tc::KNN_MAX); return IRC_E_INVAL; }
     const int nF = pl->dev.nF;
     void *fq, *fc;
@@ -117,12 +203,22 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     if (rc != IRC_OK) return rc;
     cudaError_t e = cudaMemsetAsync(pl->scratch, 0, sizeof(int), s);       // overflow-queue count
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(BF16): memset");
-    k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, (uint4 *)fq, (uint4 *)fc);
-    IRC_CHECK_LAUNCH("irc_site_knn(BF16) prep");
+    if (fp8) {
+        unsigned *amax = reinterpret_cast<unsigned *>(pl->scratch + 1);   // free word of the plan scratch
+        e = cudaMemsetAsync(amax, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(FP8): memset");
+        k_absmax<<<152 * 4, 256, 0, s>>>(F, (size_t)nF * nC, amax);
+        IRC_CHECK_LAUNCH("irc_site_knn(FP8) absmax");
+        k_prep_fp8<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, amax, (uint4 *)fq, (uint4 *)fc);
+        IRC_CHECK_LAUNCH("irc_site_knn(FP8) prep");
+    } else {
+        k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, (uint4 *)fq, (uint4 *)fc);
+        IRC_CHECK_LAUNCH("irc_site_knn(BF16) prep");
+    }
     CUtensorMap mq, mc;
-    if ((rc = make_map(&mq, fq, nF, 32)) != IRC_OK) return rc;       // 32 query rows per lane quarter
-    if ((rc = make_map(&mc, fc, nF, irc_tc::BN)) != IRC_OK) return rc;
-    rc = irc_tc::launch_knn_bf16(mq, mc, pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
+    if ((rc = make_map(&mq, fq, nF, 32, fp8)) != IRC_OK) return rc;       // 32 query rows per lane quarter
+    if ((rc = make_map(&mc, fc, nF, irc_tc::BN, fp8)) != IRC_OK) return rc;
+    rc = irc_tc::launch_knn_tc(fp8, mq, mc, pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
     if (rc != IRC_OK) return rc;
     return irc_exact_overflow_drain(pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
 }

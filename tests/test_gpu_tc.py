@@ -57,6 +57,29 @@ def test_bf16_knn_matches_exact(gpu, case):
     assert rel.max() <= 1e-4, rel.max()
 
 
+@pytest.mark.parametrize("case", [CASES[0], CASES[4]])
+def test_fp8_filter_with_exact_rerank(gpu, case):
+    """FP8-e4m3 filter (3 mantissa bits): the re-ranked entries are exact FP32
+    distances, and the kNN recall against the exact form is reported and must
+    stay above 0.95 on these clustered sites."""
+    F, plan, _ = small_site(**case)
+    Fd = torch.from_numpy(F).to(gpu)
+    P = irc.Plan(plan)
+    f8 = irc.site_knn(P, Fd, knn=30, mode="fp8")
+    ex = irc.site_knn(P, Fd, knn=30, mode="exact")
+    _lib.check(_lib.lib().irc_plan_check(P.h, irc._stream()), "irc_plan_check")
+    m8, me = f8["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy()
+    r = recall(m8, me)
+    print("fp8 recall vs exact: %.5f" % r)
+    assert r >= 0.95, r
+    same_rows = np.all(m8 == me, axis=1)
+    d8, de = f8["d2Knn"].cpu().numpy(), ex["d2Knn"].cpu().numpy()
+    assert np.array_equal(d8[same_rows].view(np.int32), de[same_rows].view(np.int32))
+    # every reported distance is the exact FP32 distance of the reported index
+    i64, _ = O.exact_knn_f64(F, plan, 30)
+    assert recall(m8, i64) >= 0.95
+
+
 def test_mass_ties_take_the_exact_fallback(gpu):
     """400 identical spikes: every query near them sees hundreds of candidates
     at one distance, so the candidate lists overflow and the exact fallback
