@@ -42,6 +42,7 @@ if ROOT not in sys.path:
 METRIC = "kNN+rho+delta spikes/s: BF16-TC vs FP32 form on one GB300 at >=99.9% kNN recall"
 WORKLOAD = "drift400k"
 KNN = 30
+TC_KNN_TRAFFIC_BYTES = 235.14e6 + 81.28e6   # ncu, one k_knn_tc launch on drift400k (read + write)
 
 
 def _dist_env():
@@ -214,8 +215,17 @@ def run_ours(args):
         if dom_ms:
             if head in ("bf16", "fp8"):
                 ach = flops / (dom_ms / 1e3) / 1e12
-                roof = {"bound": "tensor", "kernel": dom_name, "achieved": ach, "peak": peaks["bf16"],
-                        "unit": "TFLOP/s", "frac": ach / peaks["bf16"], "traffic": None,
+                # DRAM bytes (read + write) of one launch of the tensor-core kNN
+                # kernel on this exact workload, captured once with ncu
+                # (dram__bytes_read.sum + dram__bytes_write.sum, single pass).
+                traffic = TC_KNN_TRAFFIC_BYTES if (args.scale == 1.0 and world == 1) else None
+                roof = {"bound": "tensor", "kernel": "k_knn_tc (knn phase)", "achieved": ach,
+                        "peak": peaks["bf16"], "unit": "TFLOP/s", "frac": ach / peaks["bf16"],
+                        "traffic": traffic, "traffic_unit": "bytes per launch",
+                        "compulsory_bytes": 255e6 if traffic else None,
+                        "hbm_gbs_at_traffic": (traffic / (dom_ms / 1e3) / 1e9) if traffic else None,
+                        "hbm_peak_gbs": peaks["hbm"],
+                        "flops_per_pair": 2 * D,
                         "peak_src": peaks["src"] + " bf16 burst"}
             else:
                 ach = flops / (dom_ms / 1e3) / 1e12

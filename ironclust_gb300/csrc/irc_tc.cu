@@ -7,8 +7,11 @@
 // accumulators and its own epilogue warps, and the slots' candidate tiles
 // are issued round-robin so small chunks (a probe site has ~17 queries per
 // chunk) share a CTA without waiting on each other.  Items are ordered by
-// cost, largest first.  The BF16 operand rows (irc_tc_host.cu) make every
-// accumulator the approximate squared distance.  Warp roles: warp 0 issues
+// cost, largest first.  The BF16 (kind::f16) or FP8-e4m3 (kind::f8f6f4)
+// operand rows of irc_tc_host.cu -- 128 bytes each, so both use the same
+// swizzled layout and one MMA per 32 bytes -- make every accumulator the
+// approximate squared distance (FP8: a fixed positive multiple of it).
+// Warp roles: warp 0 issues
 // TMA loads (4-stage ring of 128-candidate tiles, four 32-row query boxes),
 // warp 1 owns TMEM and issues tcgen05.mma from one thread, warps 2-17 are
 // the epilogue: four per TMEM lane quarter, each reading 32 columns of
@@ -47,7 +50,6 @@ constexpr int CAPP = 64;                          // list capacity per query and
 constexpr int LROWP = CAPP + 1;                   // part-list row (u32), padded
 constexpr int BROW = BN + 1;                      // per-column minima row (f32) during the threshold step
 constexpr int EPI_WARPS = 4 * PARTS;
-constexpr int EPI_THREADS = 32 * EPI_WARPS;
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TILE_BYTES = BN * KP * 2;      // 16 KB (A tile has the same size)
 constexpr int NBUF = 4;                           // TMEM accumulator buffers, split among the slots
