@@ -170,6 +170,48 @@ int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t *q0, const 
                                int q_base, int n_out, int nF, int knn, float *vrKnn, float *rho,
                                int32_t *miKnn, float *d2Knn, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Clustering after the path: the consumers of rho, delta, nneigh and kNN.
+ * ------------------------------------------------------------------------ */
+
+/* The output normalisation of sort_ (matlab/irc2.m:3263-3264):
+ *   vrRho = vrRho / max(vrRho);  [~, ordrho] = sort(vrRho, 'descend')
+ * rho [nSpk] is normalised in place (max skips NaN; single division);
+ * ordrho [nSpk] receives 1-based spike ids in MATLAB's descending order
+ * (NaN first, equal values in index order).  Device pointers. */
+int irc_sort_rho(float *rho, int64_t *ordrho, int64_t nSpk, void *stream);
+
+/* Largest number of peaks (spikes with delta >= delta_cut) accepted by
+ * irc_assign_cluster_knn; more returns IRC_E_UNSUPPORTED. */
+#define IRC_CLUSTER_MAX_PEAKS 131072
+
+/* The cluster assignment of postCluster_ (matlab/irc2.m:6520-6535):
+ * assignCluster_knn_ (:6640-6694) -- peaks = delta >= delta_cut in
+ * descending rho order, peaks merged where their kNN lists share a spike
+ * (cell2map_, :6754-6805, including its ten-repeat cap and overwrite
+ * order), labels propagated to the other spikes along nneigh in ordrho
+ * order (at most ten in-place passes) -- then dpclus_remove_count_
+ * (:6735-6750), which drops clusters with fewer than min_count spikes.
+ *
+ * Device pointers: rho, delta [nSpk] (normalised, as sort_ leaves them);
+ * ordrho, nneigh [nSpk] 1-based spike ids; miKnn [knn x nSpk] int64
+ * column-major, the kNN list of every spike (only equality between the
+ * values matters; the reference reads the peaks' columns from its
+ * _knn_<site>.irc files).  Outputs: viClu [nSpk] int32 labels (0 = none);
+ * icl [cap] 1-based centre spike ids and vnSpk_clu [cap] spikes per cluster,
+ * first nClu entries.  counts (HOST, 3 entries) = { nClu, nClu_pre (peaks),
+ * nClu_post (clusters after the merge, before dpclus_remove_count_) }.
+ * delta_cut is compared in single precision.  Synchronises the stream.
+ *
+ * Errors: IRC_E_INVAL where MATLAB would raise an index error (an ordrho or
+ * nneigh entry it reads outside 1..nSpk), when ordrho is not a permutation
+ * of 1..nSpk (sort_ always gives one; the reference would run on without
+ * an error), or when nClu > cap (counts still filled). */
+int irc_assign_cluster_knn(int32_t *viClu, int64_t *icl, int32_t *vnSpk_clu, int64_t cap, int64_t *counts,
+                           const float *rho, const float *delta, const int64_t *ordrho,
+                           const int64_t *nneigh, const int64_t *miKnn, int knn, int64_t nSpk,
+                           float delta_cut, int min_count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

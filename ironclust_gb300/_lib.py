@@ -20,9 +20,10 @@ IRC_E_TIMEOUT = -5
 IRC_E_UNSUPPORTED = -6
 
 MODE_REF, MODE_EXACT, MODE_BF16, MODE_FP8 = 0, 1, 2, 3
+CLUSTER_MAX_PEAKS = 131072          # IRC_CLUSTER_MAX_PEAKS
 MODES = {"ref": MODE_REF, "exact": MODE_EXACT, "bf16": MODE_BF16, "fp8": MODE_FP8}
 
-_P, _I, _F = C.c_void_p, C.c_int, C.c_float
+_P, _I, _F, _L = C.c_void_p, C.c_int, C.c_float, C.c_int64
 
 # name -> argtypes (every entry returns int)
 SIGNATURES = {
@@ -41,6 +42,8 @@ SIGNATURES = {
     "irc_site_knn": [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_delta": [_P, _P, _I, _P, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_knn_exact_noalloc": [_P, _I, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P],
+    "irc_sort_rho": [_P, _P, _L, _P],
+    "irc_assign_cluster_knn": [_P, _P, _P, _L, _P, _P, _P, _P, _P, _P, _I, _L, _F, _I, _P],
 }
 
 _lib = None

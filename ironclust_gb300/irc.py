@@ -14,7 +14,8 @@ Reference call sites mirrored here:
   search_delta_drift_  matlab/irc2.m:3794-3865   -> search_delta_drift_host
   rho_paged_site_      matlab/irc2.m:3635-3680   -> rho_site
   delta_paged_site_    matlab/irc2.m:3684-3726   -> delta_site
-  sort_ normalisation  matlab/irc2.m:3263-3271   -> normalize_rho
+  sort_ normalisation  matlab/irc2.m:3263-3264   -> sort_rho
+  postCluster_         matlab/irc2.m:6520-6535   -> post_cluster, assign_cluster_knn
   cuda_knn_            matlab/irc.m:24365-24401  -> cuda_knn
   cuda_delta_knn_      matlab/irc.m:24519-24553  -> cuda_delta_knn_host
   cuda_rho_drift_      matlab/irc.m:24612-24637  -> cuda_rho_drift
@@ -305,13 +306,63 @@ def delta_post(vrDelta_times_rho, viNneigh, viSpk_out):
     return d, nn
 
 
-def normalize_rho(vrRho):
-    """vrRho / max(vrRho); ordrho = sort(vrRho, 'descend') (matlab/irc2.m:3268-3269)."""
-    r = np.asarray(vrRho, np.float32)
-    r = (r / np.float32(np.nanmax(r))).astype(np.float32)
-    key = np.where(np.isnan(r), -np.inf, r)
-    ordrho = np.argsort(-key, kind="stable") + 1
-    return r, ordrho
+def _dev_i64(x, device="cuda"):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=torch.int64).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.int64)).to(device)
+
+
+def sort_rho(vrRho):
+    """sort_'s output normalisation on the device (matlab/irc2.m:3263-3264):
+    vrRho / max(vrRho) (NaN skipped by max) and ordrho = the 1-based order of
+    sort(vrRho, 'descend') (NaN first, ties in index order).  Returns CUDA
+    tensors (float32 [n], int64 [n]); the input is not modified."""
+    r = _dev_f32(vrRho).clone()
+    order = torch.empty(r.numel(), dtype=torch.int64, device=r.device)
+    check(lib().irc_sort_rho(_p(r), _p(order), C.c_int64(r.numel()), _stream()), "irc_sort_rho")
+    return r, order
+
+
+def assign_cluster_knn(rho, delta, ordrho, nneigh, miKnn, delta_cut=1.0, min_count=0):
+    """The cluster assignment of postCluster_ (matlab/irc2.m:6520-6535):
+    assignCluster_knn_ (:6640-6694) + dpclus_remove_count_ (:6735-6750).
+
+    rho, delta: [n] normalised (as sort_ leaves them); ordrho, nneigh: [n]
+    1-based; miKnn: [n, knn] kNN ids of every spike (row s = MATLAB column
+    s).  Returns dict(viClu [n] int32, icl [nClu] int64 1-based centres,
+    vnSpk_clu [nClu] int32, nClu, nClu_pre, nClu_post); tensors on the
+    device."""
+    rho, delta = _dev_f32(rho), _dev_f32(delta)
+    dev = rho.device
+    ordrho, nneigh, mk = _dev_i64(ordrho, dev), _dev_i64(nneigh, dev), _dev_i64(miKnn, dev)
+    n = rho.numel()
+    if mk.dim() != 2 or mk.shape[0] != n:
+        raise ValueError("assign_cluster_knn: miKnn must be [nSpk, knn]")
+    viClu = torch.empty(n, dtype=torch.int32, device=dev)
+    icl = torch.empty(n, dtype=torch.int64, device=dev)
+    vn = torch.empty(n, dtype=torch.int32, device=dev)
+    counts = np.zeros(3, np.int64)
+    check(lib().irc_assign_cluster_knn(_p(viClu), _p(icl), _p(vn), C.c_int64(n),
+                                       counts.ctypes.data_as(C.c_void_p), _p(rho), _p(delta), _p(ordrho),
+                                       _p(nneigh), _p(mk), C.c_int(mk.shape[1]), C.c_int64(n),
+                                       C.c_float(delta_cut), C.c_int(min_count), _stream()),
+          "irc_assign_cluster_knn")
+    k = int(counts[0])
+    return dict(viClu=viClu, icl=icl[:k], vnSpk_clu=vn[:k], nClu=k, nClu_pre=int(counts[1]),
+                nClu_post=int(counts[2]))
+
+
+def post_cluster(S_clu, P=None):
+    """postCluster_ (matlab/irc2.m:6520-6535) on the device.  S_clu holds
+    rho, delta, ordrho, nneigh (as sort_ leaves them) and miKnn [n, knn];
+    P may set delta_cut (default 1) and min_count (default 0).  Returns the
+    S_auto fields viClu, icl, nClu, vnSpk_clu, nSpk_unique, plus nClu_pre
+    and nClu_post (the counts postCluster_ prints)."""
+    P = P or {}
+    a = assign_cluster_knn(S_clu["rho"], S_clu["delta"], S_clu["ordrho"], S_clu["nneigh"], S_clu["miKnn"],
+                           float(P.get("delta_cut", 1.0)), int(P.get("min_count", 0)))
+    a["nSpk_unique"] = int(a["vnSpk_clu"].sum().item()) if a["nClu"] else 0
+    return a
 
 
 # ---------------------------------------------------------------------------

@@ -3,7 +3,7 @@
 Three artefacts:
 
 * ``oracle/_build/libirc_oracle.so`` -- the CPU restatement in
-  ``irc_oracle.c`` (gcc, OpenMP, ``-ffp-contract=off`` so that the only fused
+  ``irc_oracle.c`` and ``irc_oracle_cluster.c`` (gcc, OpenMP, ``-ffp-contract=off`` so that the only fused
   multiply-adds are the explicit ``fmaf`` calls that restate nvcc's
   contraction of the reference kernels).
 * ``oracle/_build/libirc_refharness.so`` -- ``ref_harness.cu``, a host-only
@@ -44,11 +44,11 @@ def _stale(out, srcs):
 
 def build_oracle_lib(force=False):
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "irc_oracle.c")
+    srcs = [os.path.join(HERE, "irc_oracle.c"), os.path.join(HERE, "irc_oracle_cluster.c")]
     out = os.path.join(BUILD, "libirc_oracle.so")
-    if force or _stale(out, [src]):
-        _run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-              src, "-o", out, "-lm"])
+    if force or _stale(out, srcs):
+        _run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+             + srcs + ["-o", out, "-lm"])
     return out
 
 

@@ -11,6 +11,10 @@ calls it.
 * ``exact_knn_f64`` / ``exact_delta_f64``: double-precision ground truth.
 * ``site_knn_cpu`` / ``site_delta_cpu``: the reference CPU path (knn_cpu_,
   delta_cpu_), also the timed CPU baseline.
+* ``sort_rho`` / ``assign_cluster_knn``: the clustering step after the
+  path -- sort_'s rho normalisation and ordrho (matlab/irc2.m:3263-3264),
+  postCluster_ / assignCluster_knn_ / cell2map_ / dpclus_remove_count_
+  (matlab/irc2.m:6520-6805), restated in irc_oracle_cluster.c.
 * ``RefKernels``: the reference's own CUDA kernels (PTX built from the
   reference sources) launched with the MATLAB launch configuration on a GPU.
 """
@@ -40,8 +44,9 @@ def lib():
                      "orc_cuda_delta_knn", "orc_rho_drift", "orc_post_sort_knn", "orc_post_min",
                      "orc_exact_knn_f64", "orc_exact_delta_f64", "orc_knn_cpu", "orc_delta_cpu",
                      "orc_site_knn_cpu", "orc_site_delta_cpu", "orc_exact_knn_f32",
-                     "orc_exact_delta_f32", "orc_delta_drift"):
+                     "orc_exact_delta_f32", "orc_delta_drift", "orc_sort_rho"):
             getattr(_lib, name).restype = None
+        _lib.orc_assign_cluster_knn.restype = C.c_int
     return _lib
 
 
@@ -228,6 +233,41 @@ def site_delta_cpu(F, R, plan):
                              _ptr(q0), _ptr(nq), _ptr(roff), _ptr(rs), _ptr(rn),
                              C.c_int(len(q0)), C.c_int(qb))
     return de, nn
+
+
+# --- clustering after the path ---------------------------------------------------------
+
+def sort_rho(rho):
+    """vrRho / max(vrRho) and sort(vrRho, 'descend') order (1-based int64)."""
+    r = np.array(rho, dtype=np.float32, copy=True)
+    order = np.empty(r.size, np.int64)
+    lib().orc_sort_rho(_ptr(r), _ptr(order), C.c_int64(r.size))
+    return r, order
+
+
+def assign_cluster_knn(rho, delta, ordrho, nneigh, miKnn, delta_cut=1.0, min_count=0):
+    """postCluster_'s cluster assignment.  miKnn: [nSpk, knn] (row s = MATLAB
+    column s), any int64 ids.  Returns a dict with viClu (int32 labels, 0 =
+    none), icl (1-based centre spike ids), vnSpk_clu, nClu, nClu_pre, nClu_post;
+    raises ValueError where MATLAB would raise an index error."""
+    rho, delta = _f32(rho), _f32(delta)
+    ordrho = np.ascontiguousarray(ordrho, dtype=np.int64)
+    nneigh = np.ascontiguousarray(nneigh, dtype=np.int64)
+    mk = np.ascontiguousarray(miKnn, dtype=np.int64)
+    n = rho.size
+    knn = mk.shape[1]
+    viClu = np.empty(n, np.int32)
+    icl = np.empty(max(n, 1), np.int64)
+    vn = np.empty(max(n, 1), np.int32)
+    cnt = np.zeros(3, np.int64)
+    rc = lib().orc_assign_cluster_knn(_ptr(viClu), _ptr(icl), _ptr(vn), _ptr(cnt), _ptr(rho), _ptr(delta),
+                                      _ptr(ordrho), _ptr(nneigh), _ptr(mk), C.c_int(knn), C.c_int64(n),
+                                      C.c_float(delta_cut), C.c_int(min_count))
+    if rc != 0:
+        raise ValueError("assign_cluster_knn: index out of range")
+    k = int(cnt[0])
+    return dict(viClu=viClu, icl=icl[:k].copy(), vnSpk_clu=vn[:k].copy(), nClu=k,
+                nClu_pre=int(cnt[1]), nClu_post=int(cnt[2]))
 
 
 # --- the reference kernels on a GPU --------------------------------------------------

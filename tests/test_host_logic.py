@@ -127,8 +127,6 @@ def test_rho_and_delta_post_processing_quirks():
                            np.array([10, 20, 30]))
     assert nn.tolist() == [20, 2, 3]                          # NaN/Inf -> the spike's own local position
     assert d[1] == d[2] == irc.SQRT_SINGLE_INF_F
-    r, order = irc.normalize_rho(np.array([1, 4, 2], np.float32))
-    assert r.tolist() == [0.25, 1.0, 0.5] and order.tolist() == [2, 3, 1]
 
 
 def test_synthetic_sites_are_seeded():
