@@ -42,6 +42,7 @@ if ROOT not in sys.path:
 METRIC = "kNN+rho+delta spikes/s: BF16-TC vs FP32 form on one GB300 at >=99.9% kNN recall"
 WORKLOAD = "drift400k"
 KNN = 30
+MIN_COUNT = 30          # min_count of the reference's default parameters (matlab/default.prm:120)
 TC_KNN_TRAFFIC_BYTES = 235.14e6 + 81.28e6   # ncu, one k_knn_tc launch on drift400k (read + write)
 
 
@@ -197,6 +198,9 @@ def run_ours(args):
     e2e = None
     if not results.get(head, {}).get("error"):
         e2e = time_e2e(P, site["F"], head, args, dev, torch, irc, world, dist if world > 1 else None)
+    post = None
+    if rank == 0 and not results.get(head, {}).get("error"):
+        post, post_inputs = run_post_cluster(P, F, head, args, torch, irc, stream, flush)
     batched = None
     if args.batched and rank == 0:
         del F
@@ -254,8 +258,12 @@ def run_ours(args):
         }
         if batched is not None:
             out["batched"] = batched
+        if post is not None:
+            out["post_cluster"] = post
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(site, plan, seconds=args.cpu_seconds)
+            if post is not None:
+                post["cpu_baseline"] = post_cluster_cpu_baseline(post_inputs)
     if P is not None:
         P.close()
     if world > 1:
@@ -385,6 +393,61 @@ def time_e2e(P, F_host, mode, args, dev, torch, irc, world, dist):
     d2h = sum(h.numel() * h.element_size() for h in outs.values())
     return {"value": world * N / (ms / 1e3), "unit": "spikes/s", "ms_per_step": ms,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+
+def run_post_cluster(P, F, mode, args, torch, irc, stream, flush):
+    """The clustering step after the path on the headline form's outputs:
+    sort_'s normalisation (irc_sort_rho) and postCluster_'s assignment
+    (irc_assign_cluster_knn), device time per step (CUDA events, L2 flushed
+    before each step).  The step synchronises the host a few times (peak
+    count, merge repeats, propagation passes), which the events include."""
+    k = irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
+    N = F.shape[0]
+    rho = k["rho"]
+    # delta_paged_site_'s NaN/Inf rule and global ids (one page: identity)
+    delta = k["delta"].clone()
+    bad = ~torch.isfinite(delta)
+    delta[bad] = float(irc.SQRT_SINGLE_INF_F)
+    nneigh = torch.where(bad, torch.arange(1, N + 1, device=F.device), k["nneigh"].long())
+    mk = k["miKnn"].long()
+
+    def step():
+        rn, order = irc.sort_rho(rho)
+        return irc.assign_cluster_knn(rn, delta, order, nneigh, mk, 1.0, MIN_COUNT)
+
+    for _ in range(max(1, args.warmup)):
+        a = step()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        a = step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = sum(times) / len(times)
+    host = dict(rho=rho.cpu().numpy(), delta=delta.cpu().numpy(), nneigh=nneigh.cpu().numpy(),
+                miKnn=mk.cpu().numpy())
+    return ({"workload": "%s, %s-form rho/delta/nneigh/kNN" % (WORKLOAD, mode), "steps": args.steps,
+             "ms_per_step": ms, "spikes_per_s": N / (ms / 1e3), "delta_cut": 1.0, "min_count": MIN_COUNT,
+             "peaks": a["nClu_pre"], "clusters_after_merge": a["nClu_post"], "clusters": a["nClu"]}, host)
+
+
+def post_cluster_cpu_baseline(host):
+    """The clustering step's CPU restatement (serial, as MATLAB's loops are)
+    on the same inputs: one pass over the whole workload."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    r, o = O.sort_rho(host["rho"])
+    O.assign_cluster_knn(r, host["delta"], o, host["nneigh"], host["miKnn"], 1.0, MIN_COUNT)
+    t = time.perf_counter() - t0
+    n = host["rho"].size
+    return {"value": n / t, "unit": "spikes/s", "cores": 1, "kind": "port",
+            "sample": "the whole workload, one pass (sort_ normalisation + postCluster_ assignment)",
+            "seconds": t}
 
 
 def cpu_baseline(site, plan, seconds=15.0, chunks=None):

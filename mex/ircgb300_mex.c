@@ -10,7 +10,20 @@
  *   [K, I] = ircgb300_mex('cuda_knn_index',     B, A, vnConst, nThreads)
  *   [D, N] = ircgb300_mex('cuda_delta_knn',     B, A, R_B, R_A, vnConst, nThreads)
  *   rho    = ircgb300_mex('rho_drift',          miSite12, mrFet1, mrFet2, vnConst, dc2)
+ *   [D, N] = ircgb300_mex('delta_drift',        miSite12, mrFet1, mrFet2, vrRho1, vnConst, dc2)
+ *   [rho, ordrho] = ircgb300_mex('sort_rho',    vrRho)
+ *   [viClu, icl, vnSpk_clu, nClu_pre, nClu_post] =
+ *            ircgb300_mex('assign_cluster_knn', rho, delta, ordrho, nneigh, miKnn, delta_cut, min_count)
  *   v      = ircgb300_mex('version')
+ *
+ * sort_rho replaces `vrRho = vrRho / max(vrRho); [~, ordrho] = sort(vrRho,
+ * 'descend')` of sort_ (ordrho comes back as an int64 gpuArray; MATLAB
+ * indexes with it as with the double one).  assign_cluster_knn replaces
+ * assignCluster_knn_ + dpclus_remove_count_ inside postCluster_; ordrho,
+ * nneigh and miKnn [knn x nSpk] are int64 gpuArrays (S_clu.nneigh already
+ * is; pass int64(ordrho) and the kNN lists the path kept on the device
+ * instead of the _knn_<site>.irc files), icl and vnSpk_clu come back on the
+ * host.
  *
  * Array arguments are gpuArrays (single / int32 as the reference kernels
  * take them); vnConst may be a host or a gpuArray int32 vector (it is read on
@@ -140,6 +153,64 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         if (rc != IRC_OK) fail(rc, cmd);
         plhs[0] = mxGPUCreateMxArrayOnGPU(rho);
         mxGPUDestroyGPUArray(rho); mxGPUDestroyGPUArray(S); mxGPUDestroyGPUArray(F1); mxGPUDestroyGPUArray(F2);
+        return;
+    }
+    if (!strcmp(cmd, "delta_drift")) {
+        const mxGPUArray *S = gin(prhs[1]), *F1 = gin(prhs[2]), *F2 = gin(prhs[3]), *R = gin(prhs[4]);
+        host_i32(prhs[5], vn, 3);
+        const float dc2 = (float)mxGetScalar(prhs[6]);
+        mxGPUArray *D = gout(1, (mwSize)vn[0], mxSINGLE_CLASS);
+        mxGPUArray *N = gout(1, (mwSize)vn[0], mxUINT32_CLASS);
+        rc = irc_delta_drift((float *)mxGPUGetData(D), (uint32_t *)mxGPUGetData(N),
+                             (const int32_t *)mxGPUGetDataReadOnly(S), (const float *)mxGPUGetDataReadOnly(F1),
+                             (const float *)mxGPUGetDataReadOnly(F2), (const float *)mxGPUGetDataReadOnly(R), vn, dc2,
+                             NULL);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(D);
+        if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(N);
+        mxGPUDestroyGPUArray(D); mxGPUDestroyGPUArray(N);
+        mxGPUDestroyGPUArray(S); mxGPUDestroyGPUArray(F1); mxGPUDestroyGPUArray(F2); mxGPUDestroyGPUArray(R);
+        return;
+    }
+    if (!strcmp(cmd, "sort_rho")) {
+        const mxGPUArray *R = gin(prhs[1]);
+        const mwSize n = mxGPUGetNumberOfElements(R);
+        mxGPUArray *rho = mxGPUCopyGPUArray(R);
+        mxGPUArray *ord = gout(n, 1, mxINT64_CLASS);
+        rc = irc_sort_rho((float *)mxGPUGetData(rho), (int64_t *)mxGPUGetData(ord), (int64_t)n, NULL);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(rho);
+        if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(ord);
+        mxGPUDestroyGPUArray(rho); mxGPUDestroyGPUArray(ord); mxGPUDestroyGPUArray(R);
+        return;
+    }
+    if (!strcmp(cmd, "assign_cluster_knn")) {
+        const mxGPUArray *R = gin(prhs[1]), *De = gin(prhs[2]), *O = gin(prhs[3]), *NN = gin(prhs[4]),
+                         *K = gin(prhs[5]);
+        if (mxGPUGetClassID(O) != mxINT64_CLASS || mxGPUGetClassID(NN) != mxINT64_CLASS ||
+            mxGPUGetClassID(K) != mxINT64_CLASS)
+            mexErrMsgIdAndTxt("ircgb300:class", "assign_cluster_knn: ordrho, nneigh and miKnn must be int64");
+        const mwSize n = mxGPUGetNumberOfElements(R);
+        const int knn = (int)(mxGPUGetNumberOfElements(K) / (n ? n : 1));
+        const float cut = (float)mxGetScalar(prhs[6]);
+        const int min_count = (int)mxGetScalar(prhs[7]);
+        mxGPUArray *viClu = gout(n, 1, mxINT32_CLASS), *icl = gout(n, 1, mxINT64_CLASS),
+                   *vnc = gout(n, 1, mxINT32_CLASS);
+        int64_t counts[3] = {0, 0, 0};
+        rc = irc_assign_cluster_knn((int32_t *)mxGPUGetData(viClu), (int64_t *)mxGPUGetData(icl),
+                                    (int32_t *)mxGPUGetData(vnc), (int64_t)n, counts,
+                                    (const float *)mxGPUGetDataReadOnly(R), (const float *)mxGPUGetDataReadOnly(De),
+                                    (const int64_t *)mxGPUGetDataReadOnly(O), (const int64_t *)mxGPUGetDataReadOnly(NN),
+                                    (const int64_t *)mxGPUGetDataReadOnly(K), knn, (int64_t)n, cut, min_count, NULL);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(viClu);
+        if (nlhs > 1) { plhs[1] = mxGPUCreateMxArrayOnCPU(icl); mxSetM(plhs[1], (mwSize)counts[0]); }
+        if (nlhs > 2) { plhs[2] = mxGPUCreateMxArrayOnCPU(vnc); mxSetM(plhs[2], (mwSize)counts[0]); }
+        if (nlhs > 3) plhs[3] = mxCreateDoubleScalar((double)counts[1]);
+        if (nlhs > 4) plhs[4] = mxCreateDoubleScalar((double)counts[2]);
+        mxGPUDestroyGPUArray(viClu); mxGPUDestroyGPUArray(icl); mxGPUDestroyGPUArray(vnc);
+        mxGPUDestroyGPUArray(R); mxGPUDestroyGPUArray(De); mxGPUDestroyGPUArray(O); mxGPUDestroyGPUArray(NN);
+        mxGPUDestroyGPUArray(K);
         return;
     }
     mexErrMsgIdAndTxt("ircgb300:command", "unknown command '%s'", cmd);
