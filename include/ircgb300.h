@@ -1,10 +1,13 @@
 /*
  * ircgb300.h -- C ABI of the GB300 (sm_103a) IronClust clustering hot path.
  *
- * The library replaces the five CUDA kernels IronClust's MATLAB host launches
- * through parallel.gpu.CUDAKernel + feval, keeping their argument order,
- * array shapes and outputs, and adds fused per-site entry points that run a
- * whole site (every drift chunk) per call.
+ * The library replaces the CUDA kernels IronClust's MATLAB host launches
+ * through parallel.gpu.CUDAKernel + feval on the clustering path (the drift
+ * kNN / rho / delta kernels and their irc.m variants), keeping their
+ * argument order, array shapes and outputs; adds fused per-site entry points
+ * that run a whole site (every drift chunk) per call; and runs the
+ * clustering step that consumes their outputs (sort_'s normalisation,
+ * postCluster_'s cluster assignment).
  *
  * Conventions (identical to the reference):
  *   - feature matrices are MATLAB column-major [nC x n] float32, i.e. the nC
@@ -43,7 +46,7 @@ extern "C" {
 #define IRC_MODE_REF 0   /* bit-exact with the reference binned-minimum kernels */
 #define IRC_MODE_EXACT 1 /* true top-k, reference FP32 arithmetic, (d2, index) ties */
 #define IRC_MODE_BF16 2  /* tcgen05 BF16 distance filter + exact FP32 re-rank   */
-#define IRC_MODE_FP8 3   /* tcgen05 FP8-e4m3 filter (per-chunk scale) + re-rank */
+#define IRC_MODE_FP8 3   /* tcgen05 FP8-e4m3 filter (site-wide scale) + re-rank */
 
 int irc_version(void);                 /* 10000*major + 100*minor + patch */
 const char *irc_last_error(void);      /* message of the calling thread's last failure */
@@ -102,6 +105,52 @@ int irc_rho_drift(float *vrRho1, const int32_t *miSite12, const float *mrFet1,
 int irc_delta_drift(float *vrDelta1, uint32_t *viNneigh1, const int32_t *miSite12, const float *mrFet1,
                     const float *mrFet2, const float *vrRho1, const int32_t *vnConst, float dc2,
                     void *stream);
+
+/* The binned-minimum kNN variants of cuda_knn_index (same scan and selection
+ * sort, so results depend on nThreads the same way).  vnConst (host) =
+ * {nB, nA, nC, knn}; B: [nC x nB], A: [nC x nA]; knn <= nThreads.
+ *
+ * Replaces cuda_knn (matlab/cuda_knn.cu:24; launched from matlab/irc.m:24456
+ * with nThreads = 2 * P.nThreads = 256): K [nA] = the knn-th distance. */
+int irc_cuda_knn(float *K, const float *B, const float *A, const int32_t *vnConst, int nThreads,
+                 void *stream);
+
+/* Replaces cuda_knn_full (matlab/cuda_knn_full.cu:27; no call site in the
+ * reference's MATLAB code; its block size is 512): K [knn x nA] = every
+ * sorted distance, I [knn x nA] 1-based (1 for a bin that saw no candidate). */
+int irc_cuda_knn_full(float *K, int32_t *I, const float *B, const float *A, const int32_t *vnConst,
+                      int nThreads, void *stream);
+
+/* Replaces cuda_knn_ib (matlab/cuda_knn_ib.cu:27; no call site; block size
+ * 512): candidates are the B columns IB[0..nB-1] (1-based; B has nF
+ * columns), K [nA], I [knn x nA] = 1-based B columns.  IB entries outside
+ * 1..nF, which the reference would read out of bounds, are skipped and
+ * reported as IRC_E_INVAL (the call synchronises the stream to check). */
+int irc_cuda_knn_ib(float *K, int32_t *I, const float *B, const float *A, const int32_t *IB, int nF,
+                    const int32_t *vnConst, int nThreads, void *stream);
+
+/* Replaces jrc3_cuda_rho (matlab/irc_cuda_rho.cu:24; launched from
+ * matlab/irc.m:2551, the time-window "spacetime" clustering mode).
+ * vnConst (host) = {n1, n12, nC, dn_max, fDc_spk}; mrFet12 [nC x n12] with
+ * the n1 queries first; viiSpk12_ord [n12] time order.  vrRho1 [n1] =
+ * (candidates within |ord_i - ord_j| <= dn_max at d2 <= dc2) / (candidates
+ * within the window); fDc_spk = 1 uses d2 < dc2 * |query|^2 instead.
+ * fDc_spk must be 0 or 1 (the reference leaves its cut-off uninitialised
+ * otherwise). */
+int irc_cuda_rho(float *vrRho1, const float *mrFet12, const int32_t *viiSpk12_ord, const int32_t *vnConst,
+                 float dc2, void *stream);
+
+/* Replaces jrc3_cuda_delta (matlab/irc_cuda_delta.cu:26; irc.m's cuda_delta_,
+ * matlab/irc.m:2651-2676, names it 'iron_cuda_delta', a file the reference
+ * does not ship, so there it always falls back to the CPU).  vnConst as
+ * irc_cuda_rho; viiRho12_ord [n12] = rank in descending rho.  vrDelta1 [n1]
+ * = sqrt(min d2 / dc2) over window candidates ranked before the query (cut
+ * dc2 * |query|^2 with fDc_spk = 1); viNneigh1 [n1] 1-based into the window
+ * (the query itself when none).  nThreads = the reference block size
+ * (P.nThreads, 128): ties go to the lowest of nThreads bins; a multiple of
+ * 32 up to 128. */
+int irc_cuda_delta(float *vrDelta1, uint32_t *viNneigh1, const float *mrFet12, const int32_t *viiSpk12_ord,
+                   const int32_t *viiRho12_ord, const int32_t *vnConst, float dc2, int nThreads, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Fused per-site path.  A plan describes every launch the MATLAB chunk loop

@@ -19,6 +19,10 @@ Reference call sites mirrored here:
   cuda_knn_            matlab/irc.m:24365-24401  -> cuda_knn
   cuda_delta_knn_      matlab/irc.m:24519-24553  -> cuda_delta_knn_host
   cuda_rho_drift_      matlab/irc.m:24612-24637  -> cuda_rho_drift
+  cuda_delta_drift_    matlab/irc.m:24641-24666  -> cuda_delta_drift
+  cuda_knn__           matlab/irc.m:24437-24465  -> knn_vr
+  cuda_rho_, cuda_delta_ (time-window mode) matlab/irc.m:2528-2560, :2651-2688
+                                                 -> rho_spacetime, delta_spacetime
 """
 from __future__ import annotations
 
@@ -139,6 +143,58 @@ def delta_drift(miSite12_colmajor, mrFet1, mrFet2, vrRho12, n1, dc2):
 
 # ---------------------------------------------------------------------------
 # MATLAB post-processing on the device
+def cuda_knn_kth(B, A, knn, nThreads=256):
+    """irc_cuda_knn (cuda_knn.cu): the knn-th binned-minimum distance [nA]."""
+    K = torch.empty(A.shape[0], dtype=torch.float32, device=A.device)
+    vn = _i32host([B.shape[0], A.shape[0], A.shape[1], knn])
+    check(lib().irc_cuda_knn(_p(K), _p(B), _p(A), vn.ctypes.data_as(C.c_void_p), nThreads, _stream()),
+          "irc_cuda_knn")
+    return K
+
+
+def cuda_knn_full(B, A, knn, nThreads=512):
+    """irc_cuda_knn_full (cuda_knn_full.cu): K, I as [nA, knn] (== MATLAB [knn x nA])."""
+    nA = A.shape[0]
+    K = torch.empty((nA, knn), dtype=torch.float32, device=A.device)
+    I = torch.empty((nA, knn), dtype=torch.int32, device=A.device)
+    vn = _i32host([B.shape[0], nA, A.shape[1], knn])
+    check(lib().irc_cuda_knn_full(_p(K), _p(I), _p(B), _p(A), vn.ctypes.data_as(C.c_void_p), nThreads,
+                                  _stream()), "irc_cuda_knn_full")
+    return K, I
+
+
+def cuda_knn_ib(B, A, IB, knn, nThreads=512):
+    """irc_cuda_knn_ib (cuda_knn_ib.cu): candidates = B columns IB (1-based)."""
+    nA = A.shape[0]
+    IB = _dev_i32(IB, A.device)
+    K = torch.empty(nA, dtype=torch.float32, device=A.device)
+    I = torch.empty((nA, knn), dtype=torch.int32, device=A.device)
+    vn = _i32host([IB.numel(), nA, A.shape[1], knn])
+    check(lib().irc_cuda_knn_ib(_p(K), _p(I), _p(B), _p(A), _p(IB), B.shape[0], vn.ctypes.data_as(C.c_void_p),
+                                nThreads, _stream()), "irc_cuda_knn_ib")
+    return K, I
+
+
+def cuda_rho_st(mrFet12, ord12, n1, dn_max, dc2, fDc_spk=0):
+    """irc_cuda_rho (jrc3_cuda_rho): time-window density of the first n1 spikes."""
+    rho = torch.empty(n1, dtype=torch.float32, device=mrFet12.device)
+    vn = _i32host([n1, mrFet12.shape[0], mrFet12.shape[1], dn_max, fDc_spk])
+    check(lib().irc_cuda_rho(_p(rho), _p(mrFet12), _p(_dev_i32(ord12, mrFet12.device)),
+                             vn.ctypes.data_as(C.c_void_p), C.c_float(dc2), _stream()), "irc_cuda_rho")
+    return rho
+
+
+def cuda_delta_st(mrFet12, ord12, rr12, n1, dn_max, dc2, fDc_spk=0, nThreads=128):
+    """irc_cuda_delta (jrc3_cuda_delta): delta and nneigh (1-based) of the first n1 spikes."""
+    de = torch.empty(n1, dtype=torch.float32, device=mrFet12.device)
+    nn = torch.empty(n1, dtype=torch.int32, device=mrFet12.device)
+    vn = _i32host([n1, mrFet12.shape[0], mrFet12.shape[1], dn_max, fDc_spk])
+    check(lib().irc_cuda_delta(_p(de), _p(nn), _p(mrFet12), _p(_dev_i32(ord12, mrFet12.device)),
+                               _p(_dev_i32(rr12, mrFet12.device)), vn.ctypes.data_as(C.c_void_p),
+                               C.c_float(dc2), nThreads, _stream()), "irc_cuda_delta")
+    return de, nn
+
+
 # ---------------------------------------------------------------------------
 
 def matlab_sort_knn(D, I, knn):
@@ -410,3 +466,32 @@ def cuda_rho_drift(viSite1, viSite2, mrFet1, mrFet2, n1, dc2):
     site = torch.cat([torch.as_tensor(viSite1, dtype=torch.int32),
                       torch.as_tensor(viSite2, dtype=torch.int32)]).to(mrFet1.device)
     return rho_drift(site, mrFet1.contiguous(), mrFet2.contiguous(), n1, float(np.float32(dc2)))
+
+
+def knn_vr(mrFet, vi2, vi1, knn=30, nThreads=256):
+    """cuda_knn__ (matlab/irc.m:24437-24465): the knn-th binned-minimum
+    distance of each spike vi1 (0-based indices) among vi2, knn = min(knn, n2)."""
+    vi2 = torch.as_tensor(vi2, device=mrFet.device, dtype=torch.long)
+    vi1 = torch.as_tensor(vi1, device=mrFet.device, dtype=torch.long)
+    return cuda_knn_kth(mrFet[vi2].contiguous(), mrFet[vi1].contiguous(), min(knn, vi2.numel()), nThreads)
+
+
+def _dn_max(n1, n2, nTime_clu):
+    from .drift import matlab_round
+    return int(matlab_round((n1 + n2) / nTime_clu))
+
+
+def rho_spacetime(mrFet12, viiSpk12_ord, n1, n2, dc2, nTime_clu, fDc_spk=0):
+    """cuda_rho_ (matlab/irc.m:2528-2560), GPU branch: dn_max =
+    round((n1 + n2) / nTime_clu); mrFet12 [n12, nC] with the n1 queries first."""
+    return cuda_rho_st(mrFet12.contiguous(), viiSpk12_ord, n1, _dn_max(n1, n2, nTime_clu),
+                       float(np.float32(dc2)), fDc_spk)
+
+
+def delta_spacetime(mrFet12, viiSpk12_ord, viiRho12_ord, n1, n2, dc2, nTime_clu, fDc_spk=0, nThreads=128):
+    """cuda_delta_ (matlab/irc.m:2651-2688), GPU branch (an empty or NaN dc2
+    becomes 1, as there)."""
+    if dc2 is None or np.isnan(dc2):
+        dc2 = 1.0
+    return cuda_delta_st(mrFet12.contiguous(), viiSpk12_ord, viiRho12_ord, n1, _dn_max(n1, n2, nTime_clu),
+                         float(np.float32(dc2)), fDc_spk, nThreads)

@@ -11,6 +11,11 @@
  *   [D, N] = ircgb300_mex('cuda_delta_knn',     B, A, R_B, R_A, vnConst, nThreads)
  *   rho    = ircgb300_mex('rho_drift',          miSite12, mrFet1, mrFet2, vnConst, dc2)
  *   [D, N] = ircgb300_mex('delta_drift',        miSite12, mrFet1, mrFet2, vrRho1, vnConst, dc2)
+ *   K      = ircgb300_mex('cuda_knn',           B, A, vnConst, nThreads)
+ *   [K, I] = ircgb300_mex('cuda_knn_full',      B, A, vnConst, nThreads)
+ *   [K, I] = ircgb300_mex('cuda_knn_ib',        B, A, IB, vnConst, nThreads)
+ *   rho    = ircgb300_mex('cuda_rho',           mrFet12, viiSpk12_ord, vnConst, dc2)
+ *   [D, N] = ircgb300_mex('cuda_delta',         mrFet12, viiSpk12_ord, viiRho12_ord, vnConst, dc2, nThreads)
  *   [rho, ordrho] = ircgb300_mex('sort_rho',    vrRho)
  *   [viClu, icl, vnSpk_clu, nClu_pre, nClu_post] =
  *            ircgb300_mex('assign_cluster_knn', rho, delta, ordrho, nneigh, miKnn, delta_cut, min_count)
@@ -170,6 +175,54 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(N);
         mxGPUDestroyGPUArray(D); mxGPUDestroyGPUArray(N);
         mxGPUDestroyGPUArray(S); mxGPUDestroyGPUArray(F1); mxGPUDestroyGPUArray(F2); mxGPUDestroyGPUArray(R);
+        return;
+    }
+    if (!strcmp(cmd, "cuda_knn") || !strcmp(cmd, "cuda_knn_full") || !strcmp(cmd, "cuda_knn_ib")) {
+        const int full = !strcmp(cmd, "cuda_knn_full"), ib = !strcmp(cmd, "cuda_knn_ib");
+        const mxGPUArray *B = gin(prhs[1]), *A = gin(prhs[2]), *IB = ib ? gin(prhs[3]) : NULL;
+        host_i32(prhs[3 + ib], vn, 4);
+        const int nT = (int)mxGetScalar(prhs[4 + ib]);
+        mxGPUArray *K = full ? gout((mwSize)vn[3], (mwSize)vn[1], mxSINGLE_CLASS) : gout((mwSize)vn[1], 1, mxSINGLE_CLASS);
+        mxGPUArray *I = (full || ib) ? gout((mwSize)vn[3], (mwSize)vn[1], mxINT32_CLASS) : NULL;
+        const float *pB = (const float *)mxGPUGetDataReadOnly(B), *pA = (const float *)mxGPUGetDataReadOnly(A);
+        if (ib)
+            rc = irc_cuda_knn_ib((float *)mxGPUGetData(K), (int32_t *)mxGPUGetData(I), pB, pA,
+                                 (const int32_t *)mxGPUGetDataReadOnly(IB),
+                                 (int)(mxGPUGetNumberOfElements(B) / (mwSize)vn[2]), vn, nT, NULL);
+        else if (full)
+            rc = irc_cuda_knn_full((float *)mxGPUGetData(K), (int32_t *)mxGPUGetData(I), pB, pA, vn, nT, NULL);
+        else
+            rc = irc_cuda_knn((float *)mxGPUGetData(K), pB, pA, vn, nT, NULL);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(K);
+        if (I && nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(I);
+        mxGPUDestroyGPUArray(K);
+        if (I) mxGPUDestroyGPUArray(I);
+        mxGPUDestroyGPUArray(B); mxGPUDestroyGPUArray(A);
+        if (IB) mxGPUDestroyGPUArray(IB);
+        return;
+    }
+    if (!strcmp(cmd, "cuda_rho") || !strcmp(cmd, "cuda_delta")) {
+        const int delta = !strcmp(cmd, "cuda_delta");
+        const mxGPUArray *F = gin(prhs[1]), *O = gin(prhs[2]), *RR = delta ? gin(prhs[3]) : NULL;
+        host_i32(prhs[3 + delta], vn, 5);
+        const float dc2 = (float)mxGetScalar(prhs[4 + delta]);
+        mxGPUArray *D = gout(1, (mwSize)vn[0], mxSINGLE_CLASS);
+        mxGPUArray *N = delta ? gout(1, (mwSize)vn[0], mxUINT32_CLASS) : NULL;
+        if (delta)
+            rc = irc_cuda_delta((float *)mxGPUGetData(D), (uint32_t *)mxGPUGetData(N),
+                                (const float *)mxGPUGetDataReadOnly(F), (const int32_t *)mxGPUGetDataReadOnly(O),
+                                (const int32_t *)mxGPUGetDataReadOnly(RR), vn, dc2, (int)mxGetScalar(prhs[6]), NULL);
+        else
+            rc = irc_cuda_rho((float *)mxGPUGetData(D), (const float *)mxGPUGetDataReadOnly(F),
+                              (const int32_t *)mxGPUGetDataReadOnly(O), vn, dc2, NULL);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(D);
+        if (N && nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(N);
+        mxGPUDestroyGPUArray(D);
+        if (N) mxGPUDestroyGPUArray(N);
+        mxGPUDestroyGPUArray(F); mxGPUDestroyGPUArray(O);
+        if (RR) mxGPUDestroyGPUArray(RR);
         return;
     }
     if (!strcmp(cmd, "sort_rho")) {

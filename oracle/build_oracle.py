@@ -25,7 +25,8 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 REFERENCE_MATLAB = "/root/reference/matlab"
 REF_KERNELS = ["search_min_drift", "search_delta_drift", "cuda_knn_index",
-               "cuda_delta_knn", "irc_cuda_rho_drift", "irc_cuda_delta_drift"]
+               "cuda_delta_knn", "irc_cuda_rho_drift", "irc_cuda_delta_drift", "cuda_knn",
+               "cuda_knn_full", "cuda_knn_ib", "irc_cuda_rho", "irc_cuda_delta"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
 
@@ -72,7 +73,7 @@ def build_ref_ptx(force=False):
         out = os.path.join(REF_OUT, k + ".ptx")
         if force or _stale(out, [src]):
             jobs.append([NVCC, "-ptx", "-m64", "-arch=sm_103a", src, "-o", out])
-    with ThreadPoolExecutor(max_workers=5) as ex:
+    with ThreadPoolExecutor(max_workers=6) as ex:
         list(ex.map(_run, jobs))
     return [os.path.join(REF_OUT, k + ".ptx") for k in REF_KERNELS]
 

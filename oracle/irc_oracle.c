@@ -15,6 +15,11 @@
  *       orc_cuda_knn_index       matlab/cuda_knn_index.cu:27-111
  *       orc_cuda_delta_knn       matlab/cuda_delta_knn.cu:19-87
  *       orc_rho_drift            matlab/irc_cuda_rho_drift.cu:28-108
+ *       orc_delta_drift          matlab/irc_cuda_delta_drift.cu:28-131
+ *       orc_cuda_knn / orc_cuda_knn_full / orc_cuda_knn_ib
+ *                                matlab/cuda_knn.cu, cuda_knn_full.cu, cuda_knn_ib.cu
+ *       orc_cuda_rho / orc_cuda_delta
+ *                                matlab/irc_cuda_rho.cu, irc_cuda_delta.cu
  *     The kernels accumulate squared distances as `dist += d*d` with
  *     d = b - a in feature order; nvcc contracts that into one fused
  *     multiply-add per feature, which fmaf() restates.  This file must be
@@ -122,11 +127,17 @@ void orc_search_delta_drift(float *D, int32_t *I, const float *F, const float *R
     }
 }
 
-/* cuda_knn_index.cu:27-111.  vnConst = {nB, nA, nC, knn}.  Per-thread
- * minimum over iB = tx, tx+nT, ... (self kept), then the in-kernel selection
- * sort with swaps (not stable), K = sqrt(|k-th|), I[knn x nA]. */
-void orc_cuda_knn_index(float *K, int32_t *I, const float *B, const float *A,
-                        const int32_t *vnConst, int nT)
+/* The binned minimum + selection sort shared by cuda_knn_index.cu:27-111,
+ * cuda_knn.cu, cuda_knn_full.cu and cuda_knn_ib.cu.  vnConst = {nB, nA, nC,
+ * knn}.  Thread slot t keeps the first strict minimum over iiB = t, t+nT, ...
+ * (self kept, no d2 > 0 filter; IB, when given, maps iiB to the B column
+ * IB[iiB]-1, and the slot records that column), then knn steps of a
+ * selection sort with swaps over the nT slots (a slot holding NaN at step iK
+ * stays: nothing compares below NaN).  K: sqrt(|d|) of the knn-th slot, or of
+ * every slot 0..knn-1 when kall; I (optional): recorded column + 1, 1 for a
+ * slot that saw no candidate. */
+static void knn_bins(float *K, int32_t *I, const float *B, const float *A, const int32_t *IB,
+                     const int32_t *vnConst, int nT, int kall)
 {
     const int nB = vnConst[0], nA = vnConst[1], nC = vnConst[2], knn = vnConst[3];
 #pragma omp parallel
@@ -138,7 +149,8 @@ void orc_cuda_knn_index(float *K, int32_t *I, const float *B, const float *A,
             const float *a = A + (size_t)iA * nC;
             for (int t = 0; t < nT; ++t) { sD[t] = ORC_SINGLE_INF; sI[t] = 0; }
             for (int tx = 0; tx < nT; ++tx)
-                for (int iB = tx; iB < nB; iB += nT) {
+                for (int iiB = tx; iiB < nB; iiB += nT) {
+                    const int iB = IB ? IB[iiB] - 1 : iiB;
                     float d2 = dist2_fma(B + (size_t)iB * nC, a, nC);
                     if (d2 < sD[tx]) { sD[tx] = d2; sI[tx] = iB; }
                 }
@@ -150,11 +162,115 @@ void orc_cuda_knn_index(float *K, int32_t *I, const float *B, const float *A,
                 float tf = sD[imin]; sD[imin] = sD[iK]; sD[iK] = tf;
                 int ti = sI[imin]; sI[imin] = sI[iK]; sI[iK] = ti;
             }
-            float v = sD[knn - 1];
-            K[iA] = sqrtf(v < 0 ? -v : v);
-            for (int iK = 0; iK < knn; ++iK) I[iK + (size_t)knn * iA] = sI[iK] + 1;
+            if (kall) {
+                for (int iK = 0; iK < knn; ++iK) {
+                    float v = sD[iK];
+                    K[iK + (size_t)knn * iA] = sqrtf(v < 0 ? -v : v);
+                }
+            } else {
+                float v = sD[knn - 1];
+                K[iA] = sqrtf(v < 0 ? -v : v);
+            }
+            if (I)
+                for (int iK = 0; iK < knn; ++iK) I[iK + (size_t)knn * iA] = sI[iK] + 1;
         }
         free(sD); free(sI);
+    }
+}
+
+/* cuda_knn_index.cu:27-111: K [nA] = k-th distance, I [knn x nA]. */
+void orc_cuda_knn_index(float *K, int32_t *I, const float *B, const float *A,
+                        const int32_t *vnConst, int nT)
+{
+    knn_bins(K, I, B, A, NULL, vnConst, nT, 0);
+}
+
+/* cuda_knn.cu:24-103: K [nA] only (its index output is commented out). */
+void orc_cuda_knn(float *K, const float *B, const float *A, const int32_t *vnConst, int nT)
+{
+    knn_bins(K, NULL, B, A, NULL, vnConst, nT, 0);
+}
+
+/* cuda_knn_full.cu:27-103: K [knn x nA] (every sorted distance), I [knn x nA]. */
+void orc_cuda_knn_full(float *K, int32_t *I, const float *B, const float *A, const int32_t *vnConst,
+                       int nT)
+{
+    knn_bins(K, I, B, A, NULL, vnConst, nT, 1);
+}
+
+/* cuda_knn_ib.cu:27-103: B columns through IB (1-based, nB entries); K [nA],
+ * I [knn x nA] = IB-mapped column + 1. */
+void orc_cuda_knn_ib(float *K, int32_t *I, const float *B, const float *A, const int32_t *IB,
+                     const int32_t *vnConst, int nT)
+{
+    knn_bins(K, I, B, A, IB, vnConst, nT, 0);
+}
+
+/* Spike-specific cut-off of the fDc_spk option (irc_cuda_rho.cu:58-66,
+ * irc_cuda_delta.cu:66-73): dc2 times the query's squared norm, accumulated
+ * with fused multiply-adds in feature order, then one rounded multiply. */
+static inline float dc_spk(const float *a, int nC, float dc2)
+{
+    float v = 0.0f;
+    for (int c = 0; c < nC; ++c) v = fmaf(a[c], a[c], v);
+    return v * dc2;
+}
+
+/* irc_cuda_rho.cu:24-129 (jrc3_cuda_rho).  vnConst = {n1, n12, nC, dn_max,
+ * fDc_spk}.  Query i1 < n1 counts the candidates j < n12 within the time
+ * window |ord[i1] - ord[j]| <= dn_max (self included) and, of those, the
+ * ones at d2 <= dc2 (fDc_spk = 1: d2 < dc2 * |query|^2); rho = count /
+ * compared, divided in double.  Integer counts: no scan-order dependence. */
+void orc_cuda_rho(float *vrRho1, const float *mrFet12, const int32_t *viiSpk12_ord,
+                  const int32_t *vnConst, float dc2)
+{
+    const int n1 = vnConst[0], n12 = vnConst[1], nC = vnConst[2], dn_max = vnConst[3], fdc = vnConst[4];
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i1 = 0; i1 < n1; ++i1) {
+        const float *a = mrFet12 + (size_t)i1 * nC;
+        const float cut = fdc == 1 ? dc_spk(a, nC, dc2) : dc2;
+        long nRho = 0, nComp = 0;
+        for (int j = 0; j < n12; ++j) {
+            int dt = viiSpk12_ord[i1] - viiSpk12_ord[j];
+            if ((dt < 0 ? -dt : dt) > dn_max) continue;
+            float d2 = dist2_fma(mrFet12 + (size_t)j * nC, a, nC);
+            ++nComp;
+            if (fdc == 0 ? (d2 <= cut) : (d2 < cut)) ++nRho;
+        }
+        vrRho1[i1] = (float)((double)nRho / (double)nComp);
+    }
+}
+
+/* irc_cuda_delta.cu:26-153 (jrc3_cuda_delta).  vnConst as orc_cuda_rho;
+ * viiRho12_ord = rank in descending rho.  Candidate j of query i1 is kept
+ * when within the time window and ranked before it (viiRho12_ord[j] <
+ * viiRho12_ord[i1]).  Thread slot t of nT keeps its first strict minimum
+ * over j = t, t+nT, ...; the lowest slot holding the overall minimum wins;
+ * none below SINGLE_INF -> the query itself.  delta = sqrt(d2 / dc2)
+ * (fDc_spk = 1: / (dc2 * |query|^2)); the source's ABS applies to a
+ * non-negative value.  nneigh = index + 1. */
+void orc_cuda_delta(float *vrDelta1, uint32_t *viNneigh1, const float *mrFet12, const int32_t *viiSpk12_ord,
+                    const int32_t *viiRho12_ord, const int32_t *vnConst, float dc2, int nT)
+{
+    const int n1 = vnConst[0], n12 = vnConst[1], nC = vnConst[2], dn_max = vnConst[3], fdc = vnConst[4];
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i1 = 0; i1 < n1; ++i1) {
+        const float *a = mrFet12 + (size_t)i1 * nC;
+        float best = ORC_SINGLE_INF;
+        uint32_t bi = (uint32_t)i1;
+        for (int t = 0; t < nT; ++t) {
+            float tmin = ORC_SINGLE_INF;
+            uint32_t timin = (uint32_t)i1;
+            for (int j = t; j < n12; j += nT) {
+                int dt = viiSpk12_ord[i1] - viiSpk12_ord[j];
+                if ((dt < 0 ? -dt : dt) > dn_max || !(viiRho12_ord[j] < viiRho12_ord[i1])) continue;
+                float d2 = dist2_fma(mrFet12 + (size_t)j * nC, a, nC);
+                if (d2 < tmin) { tmin = d2; timin = (uint32_t)j; }
+            }
+            if (tmin < best) { best = tmin; bi = timin; }
+        }
+        vrDelta1[i1] = sqrtf(best / (fdc == 0 ? dc2 : dc_spk(a, nC, dc2)));
+        viNneigh1[i1] = bi + 1;
     }
 }
 

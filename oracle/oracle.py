@@ -44,7 +44,8 @@ def lib():
                      "orc_cuda_delta_knn", "orc_rho_drift", "orc_post_sort_knn", "orc_post_min",
                      "orc_exact_knn_f64", "orc_exact_delta_f64", "orc_knn_cpu", "orc_delta_cpu",
                      "orc_site_knn_cpu", "orc_site_delta_cpu", "orc_exact_knn_f32",
-                     "orc_exact_delta_f32", "orc_delta_drift", "orc_sort_rho"):
+                     "orc_exact_delta_f32", "orc_delta_drift", "orc_sort_rho", "orc_cuda_knn",
+                     "orc_cuda_knn_full", "orc_cuda_knn_ib", "orc_cuda_rho", "orc_cuda_delta"):
             getattr(_lib, name).restype = None
         _lib.orc_assign_cluster_knn.restype = C.c_int
     return _lib
@@ -97,6 +98,53 @@ def cuda_knn_index(B, A, knn, nT=512):
     I = np.empty((nA, knn), np.int32)
     lib().orc_cuda_knn_index(_ptr(K), _ptr(I), _ptr(B), _ptr(A), _ptr(vn), C.c_int(nT))
     return K, I
+
+
+def cuda_knn(B, A, knn, nT=256):
+    B, A = _fet(B), _fet(A)
+    vn = _i32([B.shape[0], A.shape[0], A.shape[1], knn])
+    K = np.empty(A.shape[0], np.float32)
+    lib().orc_cuda_knn(_ptr(K), _ptr(B), _ptr(A), _ptr(vn), C.c_int(nT))
+    return K
+
+
+def cuda_knn_full(B, A, knn, nT=512):
+    B, A = _fet(B), _fet(A)
+    nA = A.shape[0]
+    vn = _i32([B.shape[0], nA, A.shape[1], knn])
+    K = np.empty((nA, knn), np.float32)
+    I = np.empty((nA, knn), np.int32)
+    lib().orc_cuda_knn_full(_ptr(K), _ptr(I), _ptr(B), _ptr(A), _ptr(vn), C.c_int(nT))
+    return K, I
+
+
+def cuda_knn_ib(B, A, IB, knn, nT=512):
+    """IB: 1-based B columns (the candidates)."""
+    B, A, IB = _fet(B), _fet(A), _i32(IB)
+    nA = A.shape[0]
+    vn = _i32([IB.size, nA, A.shape[1], knn])
+    K = np.empty(nA, np.float32)
+    I = np.empty((nA, knn), np.int32)
+    lib().orc_cuda_knn_ib(_ptr(K), _ptr(I), _ptr(B), _ptr(A), _ptr(IB), _ptr(vn), C.c_int(nT))
+    return K, I
+
+
+def cuda_rho(mrFet12, ord12, n1, dn_max, dc2, fDc_spk=0):
+    F = _fet(mrFet12)
+    vn = _i32([n1, F.shape[0], F.shape[1], dn_max, fDc_spk])
+    rho = np.empty(n1, np.float32)
+    lib().orc_cuda_rho(_ptr(rho), _ptr(F), _ptr(_i32(ord12)), _ptr(vn), C.c_float(dc2))
+    return rho
+
+
+def cuda_delta(mrFet12, ord12, rr12, n1, dn_max, dc2, fDc_spk=0, nT=128):
+    F = _fet(mrFet12)
+    vn = _i32([n1, F.shape[0], F.shape[1], dn_max, fDc_spk])
+    de = np.empty(n1, np.float32)
+    nn = np.empty(n1, np.uint32)
+    lib().orc_cuda_delta(_ptr(de), _ptr(nn), _ptr(F), _ptr(_i32(ord12)), _ptr(_i32(rr12)), _ptr(vn),
+                         C.c_float(dc2), C.c_int(nT))
+    return de, nn
 
 
 def cuda_delta_knn(B, A, R_B, R_A, nT=128):
@@ -356,6 +404,54 @@ class RefKernels:
         self._check(self.h.refh_delta_drift(self._p(de), self._p(nn), self._p(miSite12_colmajor), self._p(mrFet1),
                                             self._p(mrFet2), self._p(rho), self._p(vn), C.c_float(dc2),
                                             C.c_int(n1), self._s()))
+        return de, nn
+
+    def cuda_knn(self, B, A, knn):
+        t = self.torch
+        nA = A.shape[0]
+        vn = t.tensor([B.shape[0], nA, A.shape[1], knn], dtype=t.int32, device=A.device)
+        K = t.zeros(nA, dtype=t.float32, device=A.device)
+        self._check(self.h.refh_cuda_knn(self._p(K), self._p(B), self._p(A), self._p(vn), C.c_int(nA), self._s()))
+        return K
+
+    def cuda_knn_full(self, B, A, knn):
+        t = self.torch
+        nA = A.shape[0]
+        vn = t.tensor([B.shape[0], nA, A.shape[1], knn], dtype=t.int32, device=A.device)
+        K = t.zeros((nA, knn), dtype=t.float32, device=A.device)
+        I = t.zeros((nA, knn), dtype=t.int32, device=A.device)
+        self._check(self.h.refh_cuda_knn_full(self._p(K), self._p(I), self._p(B), self._p(A), self._p(vn),
+                                              C.c_int(nA), self._s()))
+        return K, I
+
+    def cuda_knn_ib(self, B, A, IB, knn):
+        t = self.torch
+        nA = A.shape[0]
+        vn = t.tensor([IB.numel(), nA, A.shape[1], knn], dtype=t.int32, device=A.device)
+        K = t.zeros(nA, dtype=t.float32, device=A.device)
+        I = t.zeros((nA, knn), dtype=t.int32, device=A.device)
+        self._check(self.h.refh_cuda_knn_ib(self._p(K), self._p(I), self._p(B), self._p(A), self._p(IB),
+                                            self._p(vn), C.c_int(nA), self._s()))
+        return K, I
+
+    def cuda_rho(self, mrFet12, ord12, n1, dn_max, dc2, fDc_spk=0, nT=128):
+        t = self.torch
+        n12, nC = mrFet12.shape
+        vn = t.tensor([n1, n12, nC, dn_max, fDc_spk], dtype=t.int32, device=mrFet12.device)
+        rho = t.zeros(n1, dtype=t.float32, device=mrFet12.device)
+        self._check(self.h.refh_cuda_rho(self._p(rho), self._p(mrFet12), self._p(ord12), self._p(vn),
+                                         C.c_float(dc2), C.c_int(n1), C.c_int(nT), self._s()))
+        return rho
+
+    def cuda_delta(self, mrFet12, ord12, rr12, n1, dn_max, dc2, fDc_spk=0, nT=128):
+        t = self.torch
+        n12, nC = mrFet12.shape
+        vn = t.tensor([n1, n12, nC, dn_max, fDc_spk], dtype=t.int32, device=mrFet12.device)
+        de = t.zeros(n1, dtype=t.float32, device=mrFet12.device)
+        nn = t.zeros(n1, dtype=t.int32, device=mrFet12.device)
+        self._check(self.h.refh_cuda_delta(self._p(de), self._p(nn), self._p(mrFet12), self._p(ord12),
+                                           self._p(rr12), self._p(vn), C.c_float(dc2), C.c_int(n1),
+                                           C.c_int(nT), self._s()))
         return de, nn
 
     def rho_drift(self, miSite12_colmajor, mrFet1, mrFet2, n1, dc2):

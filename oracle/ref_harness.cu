@@ -22,6 +22,18 @@
 //                       matlab/irc.m:24522-24537
 //   jrc3_cuda_rho_drift block 128,        grid [ceil(n1/256), 16], smem 4*16*(45+1+2*128)
 //                       matlab/irc.m:24619-24631
+//   jrc3_cuda_delta_drift block 128,      grid [ceil(n1/256), 16], smem 4*16*(45+2+2*128)
+//                       matlab/irc.m:24646-24663
+//   cuda_knn            block 256,        grid [ceil(nA/256), 16], smem 4*16*(36+256)
+//                       matlab/irc.m:24440-24456 (nThreads = 2 * P.nThreads)
+//   cuda_knn_full, cuda_knn_ib
+//                       block 512,        grid [ceil(nA/16), 4],   smem 4*4*(60+2*512)
+//                       (no MATLAB call site; launched like cuda_knn_index, whose
+//                       CHUNK = 4 and NTHREADS = 512 they share)
+//   jrc3_cuda_rho       block nT (128),   grid [ceil(n1/256), 16], smem 4*16*(2+48+2*nT)
+//                       matlab/irc.m:2542-2551
+//   jrc3_cuda_delta     block nT (128),   grid [ceil(n1/256), 16], smem 4*16*(3+48+2*nT)
+//                       matlab/irc.m:2664-2673
 //
 // Every pointer argument is a device pointer, vnConst included (MATLAB passes
 // it as a gpuArray).  Each function returns a cudaError_t value (0 = ok).
@@ -33,10 +45,12 @@
 
 namespace {
 
-enum { K_MIN = 0, K_DELTA, K_KNN, K_DKNN, K_RHO, K_DDRIFT, K_COUNT };
+enum { K_MIN = 0, K_DELTA, K_KNN, K_DKNN, K_RHO, K_DDRIFT, K_CKNN, K_CKNNF, K_CKNNIB, K_SRHO, K_SDELTA, K_COUNT };
 const char *kFiles[K_COUNT] = {"search_min_drift.ptx", "search_delta_drift.ptx",
                                "cuda_knn_index.ptx", "cuda_delta_knn.ptx",
-                               "irc_cuda_rho_drift.ptx", "irc_cuda_delta_drift.ptx"};
+                               "irc_cuda_rho_drift.ptx", "irc_cuda_delta_drift.ptx",
+                               "cuda_knn.ptx", "cuda_knn_full.ptx", "cuda_knn_ib.ptx",
+                               "irc_cuda_rho.ptx", "irc_cuda_delta.ptx"};
 cudaLibrary_t g_lib[K_COUNT];
 cudaKernel_t g_kern[K_COUNT];
 bool g_loaded = false;
@@ -142,6 +156,56 @@ int refh_delta_drift(float *vrDelta1, unsigned *viNneigh1, const int *miSite12, 
     void *args[] = {&vrDelta1, &viNneigh1, &miSite12, &mrFet1, &mrFet2, &vrRho1, &vnConst_dev, &dc2};
     return (int)launch(K_DDRIFT, dim3(cdiv(n1, CHUNK * CHUNK), CHUNK), dim3(nThreads),
                        4 * CHUNK * (nC_max + 2 + 2 * nThreads), (cudaStream_t)stream, args);
+}
+
+// cuda_knn(float*K,const float*B,const float*A,const int*vnConst)
+int refh_cuda_knn(float *K, const float *B, const float *A, const int *vnConst_dev, int nA, void *stream)
+{
+    const int CHUNK = 16, nC_max = 36, nThreads = 256;
+    void *args[] = {&K, &B, &A, &vnConst_dev};
+    return (int)launch(K_CKNN, dim3(cdiv(nA, CHUNK * CHUNK), CHUNK), dim3(nThreads),
+                       4 * CHUNK * (nC_max + nThreads), (cudaStream_t)stream, args);
+}
+
+// cuda_knn_full(float*K,int*I,const float*B,const float*A,const int*vnConst)
+int refh_cuda_knn_full(float *K, int *I, const float *B, const float *A, const int *vnConst_dev, int nA,
+                       void *stream)
+{
+    const int CHUNK = 4, nC_max = 60, nThreads = 512;
+    void *args[] = {&K, &I, &B, &A, &vnConst_dev};
+    return (int)launch(K_CKNNF, dim3(cdiv(nA, CHUNK * CHUNK), CHUNK), dim3(nThreads),
+                       4 * CHUNK * (nC_max + nThreads * 2), (cudaStream_t)stream, args);
+}
+
+// cuda_knn_ib(float*K,int*I,const float*B,const float*A,const int*IB,const int*vnConst)
+int refh_cuda_knn_ib(float *K, int *I, const float *B, const float *A, const int *IB, const int *vnConst_dev,
+                     int nA, void *stream)
+{
+    const int CHUNK = 4, nC_max = 60, nThreads = 512;
+    void *args[] = {&K, &I, &B, &A, &IB, &vnConst_dev};
+    return (int)launch(K_CKNNIB, dim3(cdiv(nA, CHUNK * CHUNK), CHUNK), dim3(nThreads),
+                       4 * CHUNK * (nC_max + nThreads * 2), (cudaStream_t)stream, args);
+}
+
+// jrc3_cuda_rho(float*vrRho1,const float*mrFet12,const int*viiSpk12_ord,const int*vnConst,const float dc2)
+int refh_cuda_rho(float *vrRho1, const float *mrFet12, const int *viiSpk12_ord, const int *vnConst_dev,
+                  float dc2, int n1, int nT, void *stream)
+{
+    const int CHUNK = 16, nC_max = 48;
+    void *args[] = {&vrRho1, &mrFet12, &viiSpk12_ord, &vnConst_dev, &dc2};
+    return (int)launch(K_SRHO, dim3(cdiv(n1, CHUNK * CHUNK), CHUNK), dim3(nT),
+                       4 * CHUNK * (2 + nC_max + 2 * nT), (cudaStream_t)stream, args);
+}
+
+// jrc3_cuda_delta(float*vrDelta1,unsigned*viNneigh1,const float*mrFet12,const int*viiSpk12_ord,
+//                 const int*viiRho12_ord,const int*vnConst,const float dc2)
+int refh_cuda_delta(float *vrDelta1, unsigned *viNneigh1, const float *mrFet12, const int *viiSpk12_ord,
+                    const int *viiRho12_ord, const int *vnConst_dev, float dc2, int n1, int nT, void *stream)
+{
+    const int CHUNK = 16, nC_max = 48;
+    void *args[] = {&vrDelta1, &viNneigh1, &mrFet12, &viiSpk12_ord, &viiRho12_ord, &vnConst_dev, &dc2};
+    return (int)launch(K_SDELTA, dim3(cdiv(n1, CHUNK * CHUNK), CHUNK), dim3(nT),
+                       4 * CHUNK * (3 + nC_max + 2 * nT), (cudaStream_t)stream, args);
 }
 
 }  // extern "C"

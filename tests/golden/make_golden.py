@@ -1,6 +1,6 @@
 """Generate golden vectors from the reference's own CUDA kernels.
 
-Runs on a machine with a GPU: the five reference kernels (PTX built from
+Runs on a machine with a GPU: the reference kernels (PTX built from
 the reference sources by oracle/build_oracle.py) are launched with the
 MATLAB launch configuration through oracle/ref_harness.cu on seeded inputs
 with the edge cases the kernels meet (exact duplicates, ragged chunks,
@@ -81,6 +81,27 @@ def main(out):
     r12 = rho_with_ties(800, 26)
     de, nn = rk.delta_drift(t(np.concatenate([s1, s2])), t(f1), t(f2), t(r12), 200, float(dc2))
     g.update(ddrift_rho=r12, ddrift_delta=de.cpu().numpy(), ddrift_nn=nn.cpu().numpy())
+    # --- cuda_knn / cuda_knn_full / cuda_knn_ib -----------------------------------------
+    Bd, Ad = t(B), t(A)
+    g.update(cknn_K=rk.cuda_knn(Bd, Ad, 30).cpu().numpy())
+    K, I = rk.cuda_knn_full(Bd, Ad, 30)
+    g.update(cknnf_K=K.cpu().numpy(), cknnf_I=I.cpu().numpy())
+    IB = rng.integers(1, 701, 400).astype(np.int32)
+    IB[:5] = IB[5]
+    K, I = rk.cuda_knn_ib(Bd, Ad, t(IB), 30)
+    g.update(cknnib_IB=IB, cknnib_K=K.cpu().numpy(), cknnib_I=I.cpu().numpy())
+    # --- jrc3_cuda_rho / jrc3_cuda_delta (time window) ----------------------------------
+    F12 = rng.normal(0, 2, (900, 24)).astype(np.float32)
+    F12[3] = F12[2]
+    ordr = np.sort(rng.integers(0, 450, 900)).astype(np.int32)[rng.permutation(900)]
+    rr = (np.argsort(np.argsort(-rho_with_ties(900, 27), kind="stable"), kind="stable") + 1).astype(np.int32)
+    g.update(st_F=F12, st_ord=ordr, st_rr=rr)
+    for fdc, dcs in ((0, np.float32(4.0)), (1, np.float32(0.05))):
+        rho = rk.cuda_rho(t(F12), t(ordr), 300, 60, float(dcs), fdc)
+        de, nn = rk.cuda_delta(t(F12), t(ordr), t(rr), 300, 60, float(dcs), fdc)
+        g["st%d_dc2" % fdc] = dcs
+        g["st%d_rho" % fdc], g["st%d_delta" % fdc], g["st%d_nn" % fdc] = (
+            rho.cpu().numpy(), de.cpu().numpy(), nn.cpu().numpy())
     torch.cuda.synchronize()
     np.savez_compressed(out, **g)
     print("wrote", out, os.path.getsize(out), "bytes")

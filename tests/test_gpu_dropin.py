@@ -156,3 +156,97 @@ def test_rho_drift_bitexact(gpu, refk, n12, n1, nC):
     assert same(rho, rr)
     ro = O.rho_drift(site, f1, f2, n1, dc2)
     assert same(rho, ro)
+
+
+def _knn_inputs(nB, nA, nC, seed):
+    rng = np.random.default_rng(seed)
+    B = rng.normal(0, 3, (nB, nC)).astype(np.float32)
+    B[5] = B[4]                                                   # duplicate candidates
+    A = np.concatenate([B[:nA // 2], rng.normal(0, 3, (nA - nA // 2, nC))]).astype(np.float32)
+    return B, A
+
+
+@pytest.mark.parametrize("nB,nA,nC,knn", [(2000, 300, 33, 30), (200, 100, 24, 30), (5000, 33, 36, 16),
+                                          (100, 50, 9, 120)])
+def test_cuda_knn_bitexact(gpu, refk, nB, nA, nC, knn):
+    """cuda_knn.cu: 256 bins, K only (nB < 256 leaves empty bins)."""
+    B, A = _knn_inputs(nB, nA, nC, nB + 7)
+    knn = min(knn, nB)
+    Bd, Ad = torch.from_numpy(B).to(gpu), torch.from_numpy(A).to(gpu)
+    K = irc.cuda_knn_kth(Bd, Ad, knn)
+    assert same(K, refk.cuda_knn(Bd, Ad, knn))
+    assert same(K, O.cuda_knn(B, A, knn))
+
+
+@pytest.mark.parametrize("nB,nA,nC,knn", [(3000, 200, 33, 30), (300, 64, 60, 30), (1000, 9, 45, 200)])
+def test_cuda_knn_full_bitexact(gpu, refk, nB, nA, nC, knn):
+    B, A = _knn_inputs(nB, nA, nC, nB + 8)
+    knn = min(knn, nB)
+    Bd, Ad = torch.from_numpy(B).to(gpu), torch.from_numpy(A).to(gpu)
+    K, I = irc.cuda_knn_full(Bd, Ad, knn)
+    Kr, Ir = refk.cuda_knn_full(Bd, Ad, knn)
+    assert same(K, Kr) and same(I, Ir)
+    Ko, Io = O.cuda_knn_full(B, A, knn)
+    assert same(K, Ko) and same(I, Io)
+
+
+@pytest.mark.parametrize("nF,nB,nA,nC,knn", [(4000, 2500, 150, 33, 30), (600, 600, 40, 24, 30),
+                                             (5000, 300, 20, 60, 50)])
+def test_cuda_knn_ib_bitexact(gpu, refk, nF, nB, nA, nC, knn):
+    """Candidates through an index list with repeats and an arbitrary order."""
+    rng = np.random.default_rng(nF + nB)
+    F, A = _knn_inputs(nF, nA, nC, nF + 9)
+    IB = rng.integers(1, nF + 1, nB).astype(np.int32)
+    IB[:10] = IB[10]                                              # repeated candidates
+    Fd, Ad, IBd = (torch.from_numpy(x).to(gpu) for x in (F, A, IB))
+    K, I = irc.cuda_knn_ib(Fd, Ad, IBd, knn)
+    Kr, Ir = refk.cuda_knn_ib(Fd, Ad, IBd, knn)
+    assert same(K, Kr) and same(I, Ir)
+    Ko, Io = O.cuda_knn_ib(F, A, IB, knn)
+    assert same(K, Ko) and same(I, Io)
+
+
+def test_cuda_knn_ib_rejects_bad_index(gpu):
+    from ironclust_gb300 import _lib
+    F, A = _knn_inputs(100, 10, 8, 3)
+    IB = np.arange(1, 51, dtype=np.int32)
+    IB[7] = 101
+    with pytest.raises(_lib.IrcError):
+        irc.cuda_knn_ib(torch.from_numpy(F).to(gpu), torch.from_numpy(A).to(gpu), IB, 10)
+
+
+def _spacetime_inputs(n12, n1, nC, seed):
+    """Features with duplicates, a time order with ties, rho ranks."""
+    rng = np.random.default_rng(seed)
+    F = rng.normal(0, 2, (n12, nC)).astype(np.float32)
+    F[3] = F[2]
+    ordr = np.sort(rng.integers(0, n12 // 2, n12)).astype(np.int32)     # time order, with ties
+    perm = rng.permutation(n12)
+    F, ordr = F[perm], ordr[perm]
+    rr = np.argsort(np.argsort(-rho_with_ties(n12, seed), kind="stable"), kind="stable").astype(np.int32) + 1
+    return F, ordr, rr
+
+
+@pytest.mark.parametrize("n12,n1,nC,dn,fdc", [(1500, 400, 33, 100, 0), (800, 800, 24, 40, 1), (2000, 17, 45, 5, 0),
+                                              (300, 100, 12, 1000, 1)])
+def test_cuda_rho_spacetime_bitexact(gpu, refk, n12, n1, nC, dn, fdc):
+    F, ordr, _ = _spacetime_inputs(n12, n1, nC, n12 + dn)
+    dc2 = np.float32(4.0) if fdc == 0 else np.float32(0.05)
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(gpu)
+    rho = irc.cuda_rho_st(t(F), t(ordr), n1, dn, float(dc2), fdc)
+    assert same(rho, refk.cuda_rho(t(F), t(ordr), n1, dn, float(dc2), fdc))
+    assert same(rho, O.cuda_rho(F, ordr, n1, dn, dc2, fdc))
+
+
+@pytest.mark.parametrize("n12,n1,nC,dn,fdc,nT", [(1500, 400, 33, 100, 0, 128), (800, 800, 24, 40, 1, 128),
+                                                 (2000, 17, 45, 5, 0, 64), (300, 100, 12, 1000, 1, 32)])
+def test_cuda_delta_spacetime_bitexact(gpu, refk, n12, n1, nC, dn, fdc, nT):
+    F, ordr, rr = _spacetime_inputs(n12, n1, nC, n12 + dn + 1)
+    rr[0] = 0                                                     # a query ranked first: no candidate
+    dc2 = np.float32(4.0) if fdc == 0 else np.float32(0.05)
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(gpu)
+    de, nn = irc.cuda_delta_st(t(F), t(ordr), t(rr), n1, dn, float(dc2), fdc, nT)
+    der, nnr = refk.cuda_delta(t(F), t(ordr), t(rr), n1, dn, float(dc2), fdc, nT)
+    assert same(de, der) and same(nn, nnr)
+    deo, nno = O.cuda_delta(F, ordr, rr, n1, dn, dc2, fdc, nT)
+    assert same(de, deo) and np.array_equal(nn.cpu().numpy().view(np.uint32), nno)

@@ -63,12 +63,30 @@ def test_rho_drift_restatement(g):
 
 
 def test_delta_drift_restatement(g):
-    if "ddrift_delta" not in g:
-        pytest.skip("fixture predates the delta_drift case")
     site = np.stack([g["rho_s1"], g["rho_s2"]], 1)
     de, nn = O.delta_drift(site, g["rho_f1"], g["rho_f2"], g["ddrift_rho"], 200, float(g["rho_dc2"]))
     assert np.array_equal(bits(de), bits(g["ddrift_delta"]))
     assert np.array_equal(nn.view(np.int32), g["ddrift_nn"])
+
+
+def test_cuda_knn_variants_restatement(g):
+    B, A = g["knn_B"], g["knn_A"]
+    assert np.array_equal(bits(O.cuda_knn(B, A, 30)), bits(g["cknn_K"]))
+    K, I = O.cuda_knn_full(B, A, 30)
+    assert np.array_equal(bits(K), bits(g["cknnf_K"])) and np.array_equal(I, g["cknnf_I"])
+    K, I = O.cuda_knn_ib(B, A, g["cknnib_IB"], 30)
+    assert np.array_equal(bits(K), bits(g["cknnib_K"])) and np.array_equal(I, g["cknnib_I"])
+
+
+@pytest.mark.parametrize("fdc", [0, 1])
+def test_spacetime_rho_delta_restatement(g, fdc):
+    F, ordr, rr = g["st_F"], g["st_ord"], g["st_rr"]
+    dc2 = g["st%d_dc2" % fdc]
+    rho = O.cuda_rho(F, ordr, 300, 60, dc2, fdc)
+    assert np.array_equal(bits(rho), bits(g["st%d_rho" % fdc]))
+    de, nn = O.cuda_delta(F, ordr, rr, 300, 60, dc2, fdc)
+    assert np.array_equal(bits(de), bits(g["st%d_delta" % fdc]))
+    assert np.array_equal(nn.view(np.int32), g["st%d_nn" % fdc])
 
 
 def test_planted_mistake_is_caught(g):
