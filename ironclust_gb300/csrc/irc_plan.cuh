@@ -67,8 +67,10 @@ struct irc_plan {
     int32_t *scratch;                      // inside dmem: 4 words + 2 x n_out query lists
     const irc::TcItem *tc_items;           // inside dmem: tensor-core work items, largest first
     int n_tc_items;
-    void *tc_buf;                          // tensor-core operand rows (2 x nF x tc_row_bytes), lazily
+    void *tc_buf;                          // tensor-core operand rows (2 x nF x tc_row_bytes) and the
+                                           // padded FP32 rows of the re-rank, allocated lazily
     size_t tc_row_bytes;
+    size_t tc_bytes;                       // allocated size of tc_buf
     int ntiles[irc::kNumTileSizes];        // host copy of tile counts
     int max_nq;                            // largest query chunk
     long long pairs;                       // (query, candidate) pairs of the plan

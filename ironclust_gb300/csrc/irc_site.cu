@@ -208,20 +208,26 @@ std::vector<irc::TcItem> build_tc_items(const int32_t *q0, const int32_t *nq, co
 
 }  // namespace
 
-// Tensor-core operand rows: two [nF x row_bytes] matrices, allocated on the
-// first tensor-core call of a plan and kept until irc_plan_destroy.
-int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, size_t row_bytes)
+// Tensor-core operand rows (two [nF x row_bytes] matrices) followed by the
+// re-rank's FP32 rows padded to 16-byte multiples ([nF x fp_row_bytes]);
+// allocated on the first tensor-core call of a plan, grown when a call
+// needs more, kept until irc_plan_destroy.
+int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, void **fp, size_t row_bytes, size_t fp_row_bytes)
 {
     const size_t one = (size_t)pl->dev.nF * row_bytes;
-    if (!pl->tc_buf || pl->tc_row_bytes != row_bytes) {
+    const size_t need = 2 * one + (size_t)pl->dev.nF * fp_row_bytes;
+    if (!pl->tc_buf || pl->tc_bytes < need || pl->tc_row_bytes != row_bytes) {
         if (pl->tc_buf) cudaFree(pl->tc_buf);
         pl->tc_buf = nullptr;
-        cudaError_t e = cudaMalloc(&pl->tc_buf, 2 * one);
+        pl->tc_bytes = 0;
+        cudaError_t e = cudaMalloc(&pl->tc_buf, need);
         if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn: operand buffers");
         pl->tc_row_bytes = row_bytes;
+        pl->tc_bytes = need;
     }
     *fq = pl->tc_buf;
     *fc = (char *)pl->tc_buf + one;
+    *fp = (char *)pl->tc_buf + 2 * one;
     return IRC_OK;
 }
 

@@ -47,12 +47,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity.  On timeout the shared
-// error word is set and false returned; callers then stop their pipeline.
-// The limit (~2^22 polls with back-off, a few seconds) is far above any
-// legitimate wait of these kernels.
+// Non-blocking probe of a phase (cheaper than try_wait when the phase has
+// already completed, the common case in the pipelines below).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity: a few non-blocking
+// probes, then try_wait with back-off.  On timeout the shared error word is
+// set and false returned; callers then stop their pipeline.  The limit
+// (~2^22 polls with back-off, a few seconds) is far above any legitimate
+// wait of these kernels.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag)
 {
+    for (int f = 0; f < 64; ++f)
+        if (mbar_test_wait(bar, parity)) return true;
     for (uint32_t i = 0; i < (1u << 22); ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;

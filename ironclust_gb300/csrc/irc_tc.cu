@@ -56,8 +56,13 @@ constexpr int NBUF = 4;                           // TMEM accumulator buffers, s
 constexpr uint32_t TMEM_COLS = NBUF * BN;         // all 512 columns (one CTA per SM)
 constexpr size_t LIST_BYTES = (size_t)LROWP * PARTS * BM * 4;
 constexpr int WARP_KEYS = 64;                     // sorted re-rank keys kept per epilogue warp
+constexpr int QROW4 = 16;                         // float4 of a staged query row (nC <= 64)
+// After the passes the tile ring (A tile + STAGES candidate tiles) is idle;
+// each epilogue warp stages its re-rank candidates' rows in one share of it.
+constexpr int STAGE_F4 = (int)(TILE_BYTES * (1 + STAGES) / EPI_WARPS / 16);
 constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + TILE_BYTES * (1 + STAGES) + LIST_BYTES +
-                              EPI_WARPS * WARP_KEYS * 8 + BM * 4 /*tau*/ + PARTS * BM * 4 /*counts*/ + 256;
+                              EPI_WARPS * WARP_KEYS * 8 + EPI_WARPS * QROW4 * 16 /*query rows*/ +
+                              BM * 4 /*tau*/ + PARTS * BM * 4 /*counts*/ + 256;
 static_assert(PART == 32, "one TMEM load of 32 columns per warp and tile");
 static_assert((size_t)BROW * BM * 4 <= LIST_BYTES, "minima rows alias the list area");
 static_assert(SMEM_BYTES <= 232448, "shared memory budget");
@@ -114,20 +119,35 @@ __device__ __forceinline__ void emit(int e, unsigned long long key, int q, int k
     const bool have = key != ~0ull;
     const float d2 = have ? __uint_as_float((unsigned)(key >> 32)) : IRC_SINGLE_INF_F;
     const int idx = have ? (int)(key & 0xffffffffu) : q;
-    miKnn[(size_t)e + (size_t)knn * o] = idx + 1;
-    if (d2Knn) d2Knn[(size_t)e + (size_t)knn * o] = d2;
+    // streaming stores: the outputs are not read again by this kernel and
+    // should not push the gathered feature rows out of L2
+    __stcs(miKnn + (size_t)e + (size_t)knn * o, idx + 1);
+    if (d2Knn) __stcs(d2Knn + (size_t)e + (size_t)knn * o, d2);
     if (e == knn - 1) {
         const float vk = irc::ref_sqrt_abs(d2);
-        vrKnn[o] = vk;
-        if (rho) rho[o] = __fdiv_rn(1.0f, vk);
+        __stcs(vrKnn + o, vk);
+        if (rho) __stcs(rho + o, __fdiv_rn(1.0f, vk));
     }
 }
 
 // Exact re-rank of the candidates listed for query q in its PARTS part-lists
 // (lists[p*LROWP + i], i < cnt[p]), warp-cooperative.  Requires knn <= 32.
+// 16-byte asynchronous global -> shared copy (no register round trip), and
+// the wait for this thread's outstanding copies.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sm100::smem_u32(smem)), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 template <int PER>
 __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const int (&cnt)[PARTS], int q,
-                                       const float *__restrict__ F, int nC, int knn, size_t o,
+                                       const float *__restrict__ F, const float4 *__restrict__ Fp, int Dp4,
+                                       float4 *__restrict__ qs, float4 *__restrict__ stage, int nC, int knn, size_t o,
                                        unsigned long long *ws, int lane, int *miKnn, float *d2Knn, float *vrKnn,
                                        float *rho)
 {
@@ -135,23 +155,64 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const
     int cL = 0;
 #pragma unroll
     for (int p = 0; p < PARTS; ++p) cL += cnt[p];
+    // the query row, staged once per warp (broadcast reads below)
+    if (lane < Dp4) qs[lane] = __ldg(Fp + (size_t)q * Dp4 + lane);
+    // Exact FP32 distances with the reference arithmetic (d = b - a, fused
+    // accumulate in feature order).  Staged (stage != nullptr): candidate e is
+    // lane e % CB of batch e / CB; a batch's rows are copied into this warp's
+    // staging area with asynchronous 16-byte copies, all in flight at once
+    // (consecutive lanes copy consecutive pieces of the same rows), then each
+    // lane reads its candidate's row from shared memory.  Direct: candidate e
+    // is lane e % 32 of round e / 32 and every lane gathers its own rows.
+    const int CB = stage ? min(32, STAGE_F4 / Dp4) : 32;
+    const int nbatch = (cL + CB - 1) / CB;            // <= PER (checked by the caller)
     unsigned long long kv[PER];
 #pragma unroll
-    for (int i = 0; i < PER; ++i) {
-        const int e = i * 32 + lane;
-        kv[i] = ~0ull;
-        if (e < cL) {
+    for (int i = 0; i < PER; ++i) kv[i] = ~0ull;
+    __syncwarp();
+#pragma unroll
+    for (int bi = 0; bi < PER; ++bi) {
+        if (bi >= nbatch) break;
+        const int e = bi * CB + lane;
+        const bool has = lane < CB && e < cL;
+        int idx = q;                                  // a valid row for lanes without a candidate
+        if (has) {
             int p = 0, r = e;
 #pragma unroll
             for (int u = 0; u < PARTS - 1; ++u)
                 if (p == u && r >= cnt[u]) { r -= cnt[u]; p = u + 1; }
-            const int idx = (int)lists[p * LROWP + r];
-            const float *bb = F + (size_t)idx * nC;
-            float acc = 0.0f;
-            for (int c = 0; c < nC; ++c) acc = irc::dterm(acc, __ldg(bb + c), __ldg(a + c));
-            if (acc > 0.0f && acc < IRC_SINGLE_INF_F)
-                kv[i] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
+            idx = (int)lists[p * LROWP + r];
         }
+        const float4 *bs;
+        if (stage) {
+            const int nf = min(CB, cL - bi * CB) * Dp4; // float4 pieces of this batch
+            for (int f0 = 0; f0 < nf; f0 += 32) {         // warp-uniform trip count
+                const int f = f0 + lane;
+                const int cl = min(f / Dp4, 31), c4 = f - (f / Dp4) * Dp4;
+                const int row = __shfl_sync(0xffffffffu, idx, cl);
+                if (f < nf) cp_async16(stage + f, Fp + (size_t)row * Dp4 + c4);
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            bs = stage + lane * Dp4;
+        } else {
+            bs = Fp + (size_t)idx * Dp4;
+        }
+        if (has) {
+            float acc = 0.0f;
+#pragma unroll 3
+            for (int c4 = 0; c4 < Dp4; ++c4) {
+                const float4 av = qs[c4], bv = bs[c4];
+                const int c = 4 * c4;
+                acc = irc::dterm(acc, bv.x, av.x);
+                if (c + 1 < nC) acc = irc::dterm(acc, bv.y, av.y);
+                if (c + 2 < nC) acc = irc::dterm(acc, bv.z, av.z);
+                if (c + 3 < nC) acc = irc::dterm(acc, bv.w, av.w);
+            }
+            if (acc > 0.0f && acc < IRC_SINGLE_INF_F)
+                kv[bi] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
+        }
+        __syncwarp();
     }
     warp_bitonic<unsigned long long, PER>(kv, lane);
 #pragma unroll
@@ -245,7 +306,9 @@ __device__ __forceinline__ int chunk_tiles(const irc::PlanDev &p, int chunk)
 __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::TcItem &it, const int (&nt)[4], int qps,
                                          int bps, uint32_t tmem, uint32_t *lists, unsigned long long *wkeys,
                                          float *sTau, int *sCnt, uint64_t *acc_full, uint64_t *acc_empty,
-                                         volatile int *abort_flag, const float *__restrict__ F, int nC, int knn,
+                                         volatile int *abort_flag, const float *__restrict__ F,
+                                         const float4 *__restrict__ Fp, float4 *__restrict__ qrows,
+                                         float4 *__restrict__ ring, int nC, int knn,
                                          float *vrKnn, float *rho, int *miKnn, float *d2Knn, int *scratch, int warp,
                                          int lane)
 {
@@ -331,10 +394,12 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
         if (active && lim > 0) {
             float v[32];
             sm100::tmem_ld32(tbase + b * BN, v);
-            unsigned m = 0;
+            // four independent partial masks: short dependency chains
+            unsigned mq[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
             for (int jj = 0; jj < 32; ++jj)
-                if (v[jj] <= tau) m |= 1u << jj;
+                if (v[jj] <= tau) mq[jj & 3] |= 1u << jj;
+            unsigned m = (mq[0] | mq[1]) | (mq[2] | mq[3]);
             if (lim < 32) m &= (1u << lim) - 1u;
             if (cnt + __popc(m) > CAPP) { ovf = true; m = 0; }
             const uint32_t c0 = (uint32_t)(row0 + part * PART);
@@ -350,8 +415,19 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
     }
     sCnt[row * PARTS + part] = ovf ? -1 : cnt;
     slot_barrier(s, slot_threads);
+    // A CTA with one slot stages its re-rank candidates' rows in the tile
+    // ring: the barrier above spans all epilogue warps, so every TMA load and
+    // MMA of the CTA is complete; the ring was last written by the async
+    // proxy (TMA).  With several slots the ring may still be streaming
+    // another slot's tiles, and rows are gathered directly.
+    const bool staged = qps == 4;
+    if (staged) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     // exact re-rank: this warp serves 8 of its quarter's queries
     unsigned long long *ws = wkeys + (size_t)ew * WARP_KEYS;
+    float4 *qs = qrows + (size_t)ew * QROW4;
+    float4 *stage = staged ? ring + (size_t)ew * STAGE_F4 : nullptr;
+    const int Dp4 = (nC + 3) / 4;
+    const int CB = staged ? min(32, STAGE_F4 / Dp4) : 32;
     for (int L = 0; L < 32 / PARTS && ok; ++L) {
         const int rl = part * (32 / PARTS) + L;
         if (qrow + rl >= nq_s) break;
@@ -369,14 +445,22 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
             continue;
         }
         const int cL = c[0] + c[1] + c[2] + c[3];
+        const int nbatch = (cL + CB - 1) / CB;
+        if (nbatch > 8) {                             // (wide rows, long list) also to the fallback
+            if (lane == 0) {
+                const int k = atomicAdd(scratch + 0, 1);
+                scratch[irc::kScratchLists + k] = q;
+            }
+            continue;
+        }
         const uint32_t *lr = lists + (size_t)rowL * PARTS * LROWP;
         const size_t o = (size_t)(q - p.q_base);
-        if (cL <= 64)
-            rerank<2>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
-        else if (cL <= 128)
-            rerank<4>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        if (nbatch <= 2)
+            rerank<2>(lr, c, q, F, Fp, Dp4, qs, stage, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        else if (nbatch <= 4)
+            rerank<4>(lr, c, q, F, Fp, Dp4, qs, stage, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
         else
-            rerank<8>(lr, c, q, F, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+            rerank<8>(lr, c, q, F, Fp, Dp4, qs, stage, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
     }
 }
 
@@ -433,7 +517,7 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
 // MMA issuer (one thread), in the producer's order; slot s's tile k goes to
 // accumulator s*BPS + k % BPS.
 template <int NS, bool FP8>
-__device__ __forceinline__ void issue(const int (&nt)[4], uint32_t tmem, uint8_t *sA, uint8_t *sB, uint64_t *full,
+__device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem, uint8_t *sA, uint8_t *sB, uint64_t *full,
                                       uint64_t *empty, uint64_t *a_full, uint64_t *acc_full, uint64_t *acc_empty,
                                       uint64_t *mma_done, volatile int *abort_flag)
 {
@@ -463,7 +547,9 @@ __device__ __forceinline__ void issue(const int (&nt)[4], uint32_t tmem, uint8_t
                         const uint64_t bdesc = sm100::sdesc_sw128(sm100::smem_u32(sB + (size_t)st * TILE_BYTES));
 #pragma unroll
                         for (int kk = 0; kk < KP / 16; ++kk)
-                            if (FP8)
+                            if (kk >= nk)
+                                break;                    // the rest of every operand row is zero
+                            else if (FP8)
                                 sm100::mma_f8(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
                             else
                                 sm100::mma_f16(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
@@ -484,7 +570,8 @@ __device__ __forceinline__ void issue(const int (&nt)[4], uint32_t tmem, uint8_t
 template <bool FP8>
 __global__ void __launch_bounds__(THREADS, 1)
 k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
-              const irc_tc::TcItem *__restrict__ items, const float *__restrict__ F, int nC, int knn,
+              const irc_tc::TcItem *__restrict__ items, const float *__restrict__ F,
+              const float4 *__restrict__ Fp, int nC, int nk, int knn,
               float *__restrict__ vrKnn, float *__restrict__ rho, int *__restrict__ miKnn,
               float *__restrict__ d2Knn, int *__restrict__ scratch)
 {
@@ -494,7 +581,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
     uint8_t *sB = base + TILE_BYTES;
     uint32_t *lists = reinterpret_cast<uint32_t *>(sB + STAGES * TILE_BYTES);        // [BM][PARTS][LROWP]
     unsigned long long *wkeys = reinterpret_cast<unsigned long long *>(lists + (size_t)LROWP * PARTS * BM);
-    float *sTau = reinterpret_cast<float *>(wkeys + EPI_WARPS * WARP_KEYS);          // [BM]
+    float4 *qrows = reinterpret_cast<float4 *>(wkeys + EPI_WARPS * WARP_KEYS);       // [EPI_WARPS][QROW4]
+    float *sTau = reinterpret_cast<float *>(qrows + EPI_WARPS * QROW4);              // [BM]
     int *sCnt = reinterpret_cast<int *>(sTau + BM);                                  // [BM][PARTS], -1 = overflow
     uint64_t *bars = reinterpret_cast<uint64_t *>(sCnt + PARTS * BM);
     uint64_t *full = bars, *empty = bars + STAGES, *a_full = bars + 2 * STAGES;
@@ -534,14 +622,14 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            if (nslot == 1) issue<1, FP8>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
-            else if (nslot == 2) issue<2, FP8>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
-            else issue<4, FP8>(nt, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            if (nslot == 1) issue<1, FP8>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            else if (nslot == 2) issue<2, FP8>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            else issue<4, FP8>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
         }
         __syncwarp();
     } else {
-        epilogue(p, it, nt, qps, bps, tmem, lists, wkeys, sTau, sCnt, acc_full, acc_empty, abort_flag, F, nC, knn,
-                 vrKnn, rho, miKnn, d2Knn, scratch, warp, lane);
+        epilogue(p, it, nt, qps, bps, tmem, lists, wkeys, sTau, sCnt, acc_full, acc_empty, abort_flag, F, Fp, qrows,
+                 reinterpret_cast<float4 *>(sA), nC, knn, vrKnn, rho, miKnn, d2Knn, scratch, warp, lane);
     }
     sm100::tc_fence_before();
     __syncthreads();
@@ -556,13 +644,18 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
 
 namespace irc_tc {
 
-int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F, int nC,
-                  int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, cudaStream_t s)
+int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F,
+                  const float4 *Fp, int nC, int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn,
+                  cudaStream_t s)
 {
     auto kern = fp8 ? k_knn_tc<true> : k_knn_tc<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): smem attribute");
-    kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, F, nC, knn, vrKnn, rho,
+    // MMAs per tile: only the 32-byte K slices that hold data (nC features
+    // plus 6 BF16 / 12 FP8 norm entries); the rest of each row is zero
+    const int used = fp8 ? nC + 12 : 2 * (nC + 6);
+    const int nk = (used + 31) / 32;
+    kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, F, Fp, nC, nk, knn, vrKnn, rho,
                                                               miKnn, d2Knn, pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
     return IRC_OK;

@@ -12,7 +12,8 @@ constexpr int KP = 64;           // padded feature dimension (bf16 elements, one
 constexpr int KNN_MAX = 32;      // largest knn served (candidate lists hold >= 64 for the re-rank)
 using TcItem = irc::TcItem;
 
-int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F, int nC,
-                  int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, cudaStream_t s);
+int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F,
+                  const float4 *Fp, int nC, int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn,
+                  cudaStream_t s);
 
 }  // namespace irc_tc

@@ -20,12 +20,29 @@
 namespace {
 
 // F (f32 [nF x nC]) -> query / candidate BF16 rows of 64.
+// The re-rank's copy of a feature row: FP32, padded with zeros to Dp4
+// float4 (16-byte aligned rows, so candidate rows gather with 128-bit loads).
+__device__ __forceinline__ void write_padded_row(const float *__restrict__ a, int nC, int Dp4,
+                                                 float4 *__restrict__ out)
+{
+    for (int j = 0; j < Dp4; ++j) {
+        const int k = 4 * j;
+        float4 v;
+        v.x = k + 0 < nC ? __ldg(a + k + 0) : 0.0f;
+        v.y = k + 1 < nC ? __ldg(a + k + 1) : 0.0f;
+        v.z = k + 2 < nC ? __ldg(a + k + 2) : 0.0f;
+        v.w = k + 3 < nC ? __ldg(a + k + 3) : 0.0f;
+        out[j] = v;
+    }
+}
+
 __global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, uint4 *__restrict__ Fq,
-                            uint4 *__restrict__ Fc)
+                            uint4 *__restrict__ Fc, float4 *__restrict__ Fp, int Dp4)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nF) return;
     const float *a = F + (size_t)i * nC;
+    write_padded_row(a, nC, Dp4, Fp + (size_t)i * Dp4);
     float na = 0.0f;
     for (int k = 0; k < nC; ++k) {
         const float f = __bfloat162float(__float2bfloat16_rn(__ldg(a + k)));
@@ -96,13 +113,14 @@ constexpr int kFp8Pieces = 6;
 __device__ __forceinline__ int piece_exp(int t) { return t < 5 ? 8 - 4 * t : -9; }
 
 __global__ void k_prep_fp8(const float *__restrict__ F, int nF, int nC, const unsigned *__restrict__ amax,
-                           uint4 *__restrict__ Fq, uint4 *__restrict__ Fc)
+                           uint4 *__restrict__ Fq, uint4 *__restrict__ Fc, float4 *__restrict__ Fp, int Dp4)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nF) return;
     const float am = __uint_as_float(*amax);
     const float sc = am > 0.0f ? 32.0f / am : 1.0f;
     const float *a = F + (size_t)i * nC;
+    write_padded_row(a, nC, Dp4, Fp + (size_t)i * Dp4);
     float nx = 0.0f;
     for (int k = 0; k < nC; ++k) {
         const float x = from_e4m3(to_e4m3(sc * __ldg(a + k)));
@@ -184,7 +202,7 @@ int make_map(CUtensorMap *m, void *base, int rows, int box_rows, bool fp8)
 
 // Plan-owned tensor-core operand buffers (irc_site.cu) and the exact
 // fallback for queries whose candidate list overflowed (irc_exact.cu).
-int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, size_t row_bytes);
+int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, void **fp, size_t row_bytes, size_t fp_row_bytes);
 int irc_exact_overflow_drain(irc_plan *pl, const float *F, int nC, int knn, float *vrKnn, float *rho,
                              int32_t *miKnn, float *d2Knn, cudaStream_t s);
 
@@ -198,8 +216,9 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     }
     if (knn > irc_tc::KNN_MAX) { irc_host::set_error("irc_site_knn(BF16): knn %d > %d", knn, irc_tc::KNN_MAX); return IRC_E_INVAL; }
     const int nF = pl->dev.nF;
-    void *fq, *fc;
-    int rc = irc_plan_tc_buffers(pl, &fq, &fc, irc_tc::KP * 2);
+    void *fq, *fc, *fp;
+    const int Dp4 = (nC + 3) / 4;
+    int rc = irc_plan_tc_buffers(pl, &fq, &fc, &fp, irc_tc::KP * 2, (size_t)Dp4 * 16);
     if (rc != IRC_OK) return rc;
     cudaError_t e = cudaMemsetAsync(pl->scratch, 0, sizeof(int), s);       // overflow-queue count
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(BF16): memset");
@@ -209,16 +228,16 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
         if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(FP8): memset");
         k_absmax<<<152 * 4, 256, 0, s>>>(F, (size_t)nF * nC, amax);
         IRC_CHECK_LAUNCH("irc_site_knn(FP8) absmax");
-        k_prep_fp8<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, amax, (uint4 *)fq, (uint4 *)fc);
+        k_prep_fp8<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, amax, (uint4 *)fq, (uint4 *)fc, (float4 *)fp, Dp4);
         IRC_CHECK_LAUNCH("irc_site_knn(FP8) prep");
     } else {
-        k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, (uint4 *)fq, (uint4 *)fc);
+        k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, (uint4 *)fq, (uint4 *)fc, (float4 *)fp, Dp4);
         IRC_CHECK_LAUNCH("irc_site_knn(BF16) prep");
     }
     CUtensorMap mq, mc;
     if ((rc = make_map(&mq, fq, nF, 32, fp8)) != IRC_OK) return rc;       // 32 query rows per lane quarter
     if ((rc = make_map(&mc, fc, nF, irc_tc::BN, fp8)) != IRC_OK) return rc;
-    rc = irc_tc::launch_knn_tc(fp8, mq, mc, pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
+    rc = irc_tc::launch_knn_tc(fp8, mq, mc, pl, F, (const float4 *)fp, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
     if (rc != IRC_OK) return rc;
     return irc_exact_overflow_drain(pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
 }
