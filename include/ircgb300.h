@@ -223,6 +223,49 @@ int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t *q0, const 
  * Clustering after the path: the consumers of rho, delta, nneigh and kNN.
  * ------------------------------------------------------------------------ */
 
+/* ---------------------------------------------------------------------------
+ * On-disk formats on either side of the path (raw little-endian arrays, as
+ * MATLAB's fwrite writes them).  Paths are host strings.
+ * ------------------------------------------------------------------------ */
+
+/* load_fet_site_ (matlab/irc2.m:4039-4135) into device memory.  files
+ * [nLoads]: the per-load feature files (_fet_<load>.irc, or _fet2_ for the
+ * secondary-site features), each holding, site after site, that site's
+ * spikes as [nPc x nSitesSpk] single records (save_paged_fet_site_,
+ * matlab/irc2.m:4612-4618).  vnSpkBefore[l] / vnSpkSite[l] (host): records
+ * of the sites before this one / of this site in load l.  The site's records
+ * of all loads, concatenated in load order, are the "site records"; viSel
+ * [nOut] (DEVICE, 0-based into them; NULL = all of them in order, then nOut
+ * must equal their count) picks the output spikes.  mlPc [nPc x nSitesSpk]
+ * (host, column-major 0/1 bytes; NULL = all) selects the features, in
+ * MATLAB's linear order.  F [nC x nOut] (device, column-major) receives
+ * them; nC_out (host) = the number of selected features.  File reads are
+ * staged through pinned buffers and overlap the copies to the device.
+ * Synchronises the stream. */
+int irc_fet_load_site(float *F, int *nC_out, const char *const *files, int nLoads, const int64_t *vnSpkBefore,
+                      const int64_t *vnSpkSite, int nPc, int nSitesSpk, const uint8_t *mlPc, const int64_t *viSel,
+                      int64_t nOut, void *stream);
+
+/* The kNN file of rho_paged_site_ / save_miKnn_site_ (matlab/irc2.m:3670-3679,
+ * :3355-3370): miKnn [knnIn x n] (device, 1-based positions into the site
+ * feature matrix, as irc_site_knn returns them), viSpk [nF] (device, int64
+ * global spike ids of the feature-matrix columns) -> int64 [knnOut x n]
+ * global ids, rows padded to knnOut by repeating the last, written to path
+ * (append != 0: appended, as for every page after the first).  Synchronises
+ * the stream. */
+int irc_knn_save_site(const char *path, int append, const int32_t *miKnn, int knnIn, int knnOut, int64_t n,
+                      const int64_t *viSpk, int64_t nF, void *stream);
+
+/* The sort result file of sort_cache_ / struct_save_bin_ (matlab/irc2.m:356-391,
+ * :1733-1750): rho, delta (single), nneigh (int64), ordrho (written as
+ * double, as MATLAB's sort returns it) concatenated; device arrays of nSpk.
+ * irc_sort_load reads the same layout back (ordrho to int64).  Both
+ * synchronise the stream. */
+int irc_sort_save(const char *path, const float *rho, const float *delta, const int64_t *nneigh,
+                  const int64_t *ordrho, int64_t nSpk, void *stream);
+int irc_sort_load(const char *path, float *rho, float *delta, int64_t *nneigh, int64_t *ordrho, int64_t nSpk,
+                  void *stream);
+
 /* The drift linkage of calc_drift_ (matlab/irc2.m:6373-6465) on the device.
  * vrAmp, vrPos [nSpk] (device): spike amplitudes and positions (second
  * column of mrPos_spk).  Chunks of equal spike counts, viLim [n+1] int64

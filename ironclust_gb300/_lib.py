@@ -48,6 +48,10 @@ SIGNATURES = {
     "irc_cuda_rho": [_P, _P, _P, _P, _F, _P],
     "irc_cuda_delta": [_P, _P, _P, _P, _P, _P, _F, _I, _P],
     "irc_calc_drift": [_P, _P, _P, _P, _P, _L, _I, _I, _I, _I, _I, _P],
+    "irc_fet_load_site": [_P, _P, _P, _I, _P, _P, _I, _I, _P, _P, _L, _P],
+    "irc_knn_save_site": [C.c_char_p, _I, _P, _I, _I, _L, _P, _L, _P],
+    "irc_sort_save": [C.c_char_p, _P, _P, _P, _P, _L, _P],
+    "irc_sort_load": [C.c_char_p, _P, _P, _P, _P, _L, _P],
     "irc_sort_rho": [_P, _P, _L, _P],
     "irc_assign_cluster_knn": [_P, _P, _P, _L, _P, _P, _P, _P, _P, _P, _I, _L, _F, _I, _P],
 }

@@ -21,6 +21,9 @@
  *   [rho, ordrho] = ircgb300_mex('sort_rho',    vrRho)
  *   [viClu, icl, vnSpk_clu, nClu_pre, nClu_post] =
  *            ircgb300_mex('assign_cluster_knn', rho, delta, ordrho, nneigh, miKnn, delta_cut, min_count)
+ *   F      = ircgb300_mex('fet_load_site',      csFiles_fet, vnSpkBefore, vnSpkSite, dimm_fet, mlPc [, viSel])
+ *            ircgb300_mex('knn_save_site',      vcFile_knn, fAppend, miKnn, viSpk_out, knn)
+ *            ircgb300_mex('sort_save',          vcFile, rho, delta, nneigh, ordrho)
  *   v      = ircgb300_mex('version')
  *
  * sort_rho replaces `vrRho = vrRho / max(vrRho); [~, ordrho] = sort(vrRho,
@@ -246,6 +249,67 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         mxSetN(plhs[0], (mwSize)n);
         if (nlhs > 1) { plhs[1] = mxGPUCreateMxArrayOnCPU(lim); mxSetM(plhs[1], (mwSize)n + 1); }
         mxGPUDestroyGPUArray(mi); mxGPUDestroyGPUArray(lim); mxGPUDestroyGPUArray(A); mxGPUDestroyGPUArray(P);
+        return;
+    }
+    if (!strcmp(cmd, "fet_load_site")) {
+        /* csFiles_fet: cell of load file names; vnSpkBefore, vnSpkSite: double
+         * vectors per load; dimm_fet = [nPc, nSites_spk]; mlPc logical;
+         * viSel: optional int64 gpuArray, 0-based into the site's records */
+        const mxArray *cs = prhs[1];
+        const int nLoads = (int)mxGetNumberOfElements(cs);
+        char **names = (char **)mxCalloc((size_t)nLoads, sizeof(char *));
+        int64_t *bef = (int64_t *)mxCalloc((size_t)nLoads, sizeof(int64_t));
+        int64_t *cnt = (int64_t *)mxCalloc((size_t)nLoads, sizeof(int64_t));
+        int64_t nRec = 0;
+        for (int l = 0; l < nLoads; ++l) {
+            names[l] = mxArrayToString(mxGetCell(cs, (mwIndex)l));
+            bef[l] = (int64_t)mxGetPr(prhs[2])[l];
+            cnt[l] = (int64_t)mxGetPr(prhs[3])[l];
+            nRec += cnt[l];
+        }
+        const int nPc = (int)mxGetPr(prhs[4])[0], nSitesSpk = (int)mxGetPr(prhs[4])[1];
+        const mxLogical *ml = mxGetNumberOfElements(prhs[5]) ? mxGetLogicals(prhs[5]) : NULL;
+        int nC = nPc * nSitesSpk;
+        if (ml) { nC = 0; for (int i = 0; i < nPc * nSitesSpk; ++i) nC += ml[i] ? 1 : 0; }
+        const mxGPUArray *sel = nrhs > 6 ? gin(prhs[6]) : NULL;
+        const int64_t nOut = sel ? (int64_t)mxGPUGetNumberOfElements(sel) : nRec;
+        mxGPUArray *F = gout((mwSize)nC, (mwSize)nOut, mxSINGLE_CLASS);
+        int ncOut = 0;
+        rc = irc_fet_load_site((float *)mxGPUGetData(F), &ncOut, (const char *const *)names, nLoads, bef, cnt, nPc,
+                               nSitesSpk, (const uint8_t *)ml, sel ? (const int64_t *)mxGPUGetDataReadOnly(sel) : NULL,
+                               nOut, NULL);
+        for (int l = 0; l < nLoads; ++l) mxFree(names[l]);
+        mxFree(names); mxFree(bef); mxFree(cnt);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(F);
+        mxGPUDestroyGPUArray(F);
+        if (sel) mxGPUDestroyGPUArray(sel);
+        return;
+    }
+    if (!strcmp(cmd, "knn_save_site")) {
+        char *path = mxArrayToString(prhs[1]);
+        const int fAppend = (int)mxGetScalar(prhs[2]);
+        const mxGPUArray *K = gin(prhs[3]), *V = gin(prhs[4]);
+        const int knn = (int)mxGetScalar(prhs[5]);
+        const mwSize *dk = mxGPUGetDimensions(K);
+        rc = irc_knn_save_site(path, fAppend, (const int32_t *)mxGPUGetDataReadOnly(K), (int)dk[0], knn,
+                               (int64_t)dk[1], (const int64_t *)mxGPUGetDataReadOnly(V),
+                               (int64_t)mxGPUGetNumberOfElements(V), NULL);
+        mxFree((void *)dk);
+        mxFree(path);
+        mxGPUDestroyGPUArray(K); mxGPUDestroyGPUArray(V);
+        if (rc != IRC_OK) fail(rc, cmd);
+        return;
+    }
+    if (!strcmp(cmd, "sort_save")) {
+        char *path = mxArrayToString(prhs[1]);
+        const mxGPUArray *R = gin(prhs[2]), *D = gin(prhs[3]), *NN = gin(prhs[4]), *O = gin(prhs[5]);
+        rc = irc_sort_save(path, (const float *)mxGPUGetDataReadOnly(R), (const float *)mxGPUGetDataReadOnly(D),
+                           (const int64_t *)mxGPUGetDataReadOnly(NN), (const int64_t *)mxGPUGetDataReadOnly(O),
+                           (int64_t)mxGPUGetNumberOfElements(R), NULL);
+        mxFree(path);
+        mxGPUDestroyGPUArray(R); mxGPUDestroyGPUArray(D); mxGPUDestroyGPUArray(NN); mxGPUDestroyGPUArray(O);
+        if (rc != IRC_OK) fail(rc, cmd);
         return;
     }
     if (!strcmp(cmd, "sort_rho")) {

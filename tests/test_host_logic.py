@@ -146,3 +146,25 @@ def test_lpt_site_assignment():
     assert shard.imbalance(costs, a) < 1.15
     assert shard.assign_sites(costs, 3) == a                 # deterministic
     assert shard.assign_sites(costs, 1) == [list(range(8))]
+
+
+def test_fet_selection_matches_reference_reader(tmp_path):
+    """The host side of load_fet_site_ (which record of which load) picks the
+    records the reference reader returns."""
+    from ironclust_gb300 import files
+    from oracle import io_oracle as IO
+    rng = np.random.default_rng(2)
+    tr = [rng.normal(size=(n, 4, 3)).astype(np.float32) for n in (300, 0, 500)]
+    site = [rng.integers(0, 4, len(x)) for x in tr]
+    fs, cc = IO.write_fet_files(str(tmp_path / "r"), tr, site, 4)
+    recs = []
+    for path, load in zip(fs, cc):
+        raw = np.fromfile(path, np.float32).reshape(-1, 12)
+        recs.append(raw)
+    for s in range(4):
+        everyone = np.concatenate([load[s] for load in cc])
+        vi = np.sort(rng.choice(everyone, len(everyone) // 2, replace=False))
+        before, counts, sel, spikes = files.fet_selection(cc, s, vi)
+        site_recs = np.concatenate([r[b:b + c] for r, b, c in zip(recs, before, counts)])
+        assert np.array_equal(site_recs[sel], IO.load_fet_site(fs, cc, s, vi, 3, 4))
+        assert np.array_equal(spikes, vi)
