@@ -43,7 +43,7 @@ METRIC = "kNN+rho+delta spikes/s: BF16-TC vs FP32 form on one GB300 at >=99.9% k
 WORKLOAD = "drift400k"
 KNN = 30
 MIN_COUNT = 30          # min_count of the reference's default parameters (matlab/default.prm:120)
-TC_KNN_TRAFFIC_BYTES = 235.14e6 + 81.28e6   # ncu, one k_knn_tc launch on drift400k (read + write)
+TC_KNN_TRAFFIC_BYTES = 244.47e6 + 82.23e6   # ncu, one k_knn_tc launch on drift400k (read + write)
 
 
 def _dist_env():
@@ -226,7 +226,7 @@ def run_ours(args):
                 roof = {"bound": "tensor", "kernel": "k_knn_tc (knn phase)", "achieved": ach,
                         "peak": peaks["bf16"], "unit": "TFLOP/s", "frac": ach / peaks["bf16"],
                         "traffic": traffic, "traffic_unit": "bytes per launch",
-                        "compulsory_bytes": 255e6 if traffic else None,
+                        "compulsory_bytes": 259e6 if traffic else None,
                         "hbm_gbs_at_traffic": (traffic / (dom_ms / 1e3) / 1e9) if traffic else None,
                         "hbm_peak_gbs": peaks["hbm"],
                         "flops_per_pair": 2 * D,
