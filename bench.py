@@ -148,7 +148,14 @@ def run_ours(args):
     head = args.mode if args.mode in forms else forms[0]
     results = {}
     kernel_ms = {}
+    from ironclust_gb300 import autotune
+    tuned = {}
     for mode in forms:
+        if mode in ("bf16", "fp8"):
+            t = autotune.tune(P, F, KNN, mode, use_cache=False)
+            tuned[mode] = {"layout": {"max_slots": t["layout"][0], "order": t["layout"][1]},
+                           "knn_ms": {"%d,%d" % k: v for k, v in t["ms"].items()}}
+
         def step():
             return irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
         try:
@@ -250,6 +257,7 @@ def run_ours(args):
                        "l2": "flushed (256 MB write) before every timed step"},
             "forms": {m: {k: v for k, v in r.items() if k != "clocks"} for m, r in results.items()},
             "kernel_ms": kernel_ms,
+            "autotune": tuned,
             "recall_vs_exact": recall,
             "clocks": hr.get("clocks"),
             "e2e": e2e,
@@ -287,8 +295,14 @@ def run_batched(args, dev, torch, irc, flush, stream):
     res = {"workload": "probe10m" if args.probe_sites == 384 else "probe%d" % args.probe_sites,
            "sites": b.n_sites, "spikes": N, "chunks": int(len(b.plan["q0"])), "pairs": plan_pairs(b.plan),
            "dims": sorted(set(int(d) for d in b.dims)), "generation_s": gen_s, "forms": {}}
+    from ironclust_gb300 import autotune
     outs = {}
     for mode in [m.strip() for m in args.batched_forms.split(",") if m.strip()]:
+        tuned = None
+        if mode in ("bf16", "fp8"):
+            t = autotune.tune(P, F, KNN, mode, use_cache=False)
+            tuned = {"layout": {"max_slots": t["layout"][0], "order": t["layout"][1]},
+                     "knn_ms": {"%d,%d" % k: v for k, v in t["ms"].items()}}
         for _ in range(2):
             irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
         torch.cuda.synchronize()
@@ -321,6 +335,8 @@ def run_batched(args, dev, torch, irc, flush, stream):
         ms_e, ms_g = sum(eager) / len(eager), sum(graph) / len(graph)
         res["forms"][mode] = {"ms_eager": ms_e, "ms_graph": ms_g, "spikes_per_s_graph": N / (ms_g / 1e3),
                               "spikes_per_s_eager": N / (ms_e / 1e3)}
+        if tuned:
+            res["forms"][mode]["autotune"] = tuned
         outs[mode] = out["miKnn"].clone()
         del g
     if "exact" in outs:

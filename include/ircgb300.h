@@ -174,6 +174,15 @@ int irc_plan_destroy(irc_plan *plan);
  * flag.  No reference counterpart: the reference kernels have no waits. */
 int irc_plan_check(irc_plan *plan, void *stream);
 
+/* Layout of the plan's tensor-core work items (IRC_MODE_BF16 / FP8): chunks
+ * with more than 64 queries run as 128-query CTAs; the remaining queries of
+ * each chunk are packed up to max_slots chunks per CTA (1, 2 or 4; default
+ * 4); order 0 = costliest first with a chunk's CTAs adjacent (default),
+ * 1 = chunk order.  Results do not depend on the layout, only speed does
+ * (ironclust_gb300.autotune picks it by timing).  Synchronises the device;
+ * call it outside stream capture.  No reference counterpart. */
+int irc_plan_tc_layout(irc_plan *plan, int max_slots, int order);
+
 /* kNN + rho of every query of the plan (rho_paged_site_ up to the global-id
  * mapping, matlab/irc2.m:3645-3670).
  * vrKnn [n_out]: distance of the knn-th neighbour; rho [n_out] (optional) =

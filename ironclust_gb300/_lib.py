@@ -39,6 +39,7 @@ SIGNATURES = {
     "irc_plan_create": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I],
     "irc_plan_destroy": [_P],
     "irc_plan_check": [_P, _P],
+    "irc_plan_tc_layout": [_P, _I, _I],
     "irc_site_knn": [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_delta": [_P, _P, _I, _P, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_knn_exact_noalloc": [_P, _I, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P],

@@ -65,8 +65,9 @@ struct irc_plan {
     irc::PlanDev dev;
     void *dmem;                            // single device allocation behind dev
     int32_t *scratch;                      // inside dmem: 4 words + 2 x n_out query lists
-    const irc::TcItem *tc_items;           // inside dmem: tensor-core work items, largest first
+    const irc::TcItem *tc_items;           // tensor-core work items: inside dmem, or tc_items_buf
     int n_tc_items;
+    void *tc_items_buf;                    // items of irc_plan_tc_layout, when called
     void *tc_buf;                          // tensor-core operand rows (2 x nF x tc_row_bytes) and the
                                            // padded FP32 rows of the re-rank, allocated lazily
     size_t tc_row_bytes;

@@ -154,8 +154,14 @@ struct Slot {
 
 // Work items of the tensor-core kNN (see irc_tc.cu).  Cost of an item: the
 // largest candidate-tile count among its slots (its slots run side by side).
+// Layout: chunks with more than 64 queries (more than 0 with max_slots == 1)
+// are cut into 128-row single-slot items; the remainders are packed two
+// (64-row slots) or four (32-row slots) per item, at most max_slots, slots of
+// similar tile counts together.  order 0: items by cost, largest first, the
+// items of one chunk adjacent (they stream the same candidate tiles and share
+// them in L2); order 1: chunk order.
 std::vector<irc::TcItem> build_tc_items(const int32_t *q0, const int32_t *nq, const int32_t *roff,
-                                        const int32_t *rn, int nChunks)
+                                        const int32_t *rn, int nChunks, int max_slots, int order_mode)
 {
     std::vector<irc::TcItem> items;
     std::vector<int> cost;
@@ -174,17 +180,18 @@ std::vector<irc::TcItem> build_tc_items(const int32_t *q0, const int32_t *nq, co
         items.push_back(it);
         cost.push_back(c);
     };
+    const int big = max_slots == 1 ? 0 : 64;         // remainders up to this many rows are packed
     for (int i = 0; i < nChunks; ++i) {
         int nt = 0;
         for (int r = roff[i]; r < roff[i + 1]; ++r) nt += (rn[r] + 127) / 128;
         int q = q0[i], R = nq[i];
-        while (R > 64) {
+        while (R > big) {
             const Slot s{i, q, std::min(128, R), nt};
             push(1, &s, 1);
             q += s.nq;
             R -= s.nq;
         }
-        if (R > 32) s2.push_back(Slot{i, q, R, nt});
+        if (R > 32 || (R > 0 && max_slots == 2)) s2.push_back(Slot{i, q, R, nt});
         else if (R > 0) s1.push_back(Slot{i, q, R, nt});
     }
     auto by_nt = [](const Slot &a, const Slot &b) { return a.nt > b.nt || (a.nt == b.nt && a.chunk < b.chunk); };
@@ -194,16 +201,34 @@ std::vector<irc::TcItem> build_tc_items(const int32_t *q0, const int32_t *nq, co
     for (size_t k = 0; k < s1.size(); k += 4) push(4, &s1[k], (int)std::min<size_t>(4, s1.size() - k));
     std::vector<int> order(items.size());
     for (size_t k = 0; k < order.size(); ++k) order[k] = (int)k;
-    // largest first; items of one chunk stay adjacent so the CTAs that stream
-    // the same candidate tiles run together and share them in L2
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        if (cost[a] != cost[b]) return cost[a] > cost[b];
-        return items[a].chunk[0] < items[b].chunk[0];
-    });
+    if (order_mode == 0)
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            if (cost[a] != cost[b]) return cost[a] > cost[b];
+            return items[a].chunk[0] < items[b].chunk[0];
+        });
+    else
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return items[a].chunk[0] < items[b].chunk[0]; });
     std::vector<irc::TcItem> out;
     out.reserve(items.size());
     for (int k : order) out.push_back(items[k]);
     return out;
+}
+
+// Adjacent runs of a chunk merged into candidate intervals (same candidate set).
+void merge_runs(const int32_t *roff, const int32_t *rs, const int32_t *rn, int nChunks, std::vector<int32_t> &moff,
+                std::vector<int32_t> &ms, std::vector<int32_t> &mn)
+{
+    moff.assign(1, 0);
+    ms.clear();
+    mn.clear();
+    for (int i = 0; i < nChunks; ++i) {
+        for (int r = roff[i]; r < roff[i + 1]; ++r) {
+            if ((int)ms.size() > moff.back() && ms.back() + mn.back() == rs[r]) mn.back() += rn[r];
+            else { ms.push_back(rs[r]); mn.push_back(rn[r]); }
+        }
+        moff.push_back((int32_t)ms.size());
+    }
 }
 
 }  // namespace
@@ -353,14 +378,8 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     size_t off_q0 = img.size(); img.insert(img.end(), q0, q0 + nCh);
     size_t off_nq = img.size(); img.insert(img.end(), nq, nq + nCh);
     // candidate intervals: adjacent runs of a chunk merged (same candidate set)
-    std::vector<int32_t> moff(1, 0), ms, mn;
-    for (int i = 0; i < nChunks; ++i) {
-        for (int r = roff[i]; r < roff[i + 1]; ++r) {
-            if ((int)ms.size() > moff.back() && ms.back() + mn.back() == rs[r]) mn.back() += rn[r];
-            else { ms.push_back(rs[r]); mn.push_back(rn[r]); }
-        }
-        moff.push_back((int32_t)ms.size());
-    }
+    std::vector<int32_t> moff, ms, mn;
+    merge_runs(roff, rs, rn, nChunks, moff, ms, mn);
     size_t off_roff = img.size(); img.insert(img.end(), moff.begin(), moff.end());
     size_t off_rs = img.size(); img.insert(img.end(), ms.begin(), ms.end());
     size_t off_rn = img.size(); img.insert(img.end(), mn.begin(), mn.end());
@@ -379,7 +398,7 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     // tensor-core work items: 128-row tiles of large chunks, then the 33-64 and
     // 1-32 row remainders packed two and four per item (similar tile counts
     // together), all ordered by cost, largest first
-    std::vector<irc::TcItem> items = build_tc_items(q0, nq, moff.data(), mn.data(), nChunks);
+    std::vector<irc::TcItem> items = build_tc_items(q0, nq, moff.data(), mn.data(), nChunks, 4, 0);
     while (img.size() % 16) img.push_back(0);
     const size_t off_items = img.size();
     for (const irc::TcItem &it : items) {
@@ -430,9 +449,36 @@ int irc_plan_destroy(irc_plan *pl)
     if (!pl) return IRC_OK;
     cudaError_t e = cudaFree(pl->dmem);
     if (pl->tc_buf) cudaFree(pl->tc_buf);
+    if (pl->tc_items_buf) cudaFree(pl->tc_items_buf);
     free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn);
     free(pl);
     return e == cudaSuccess ? IRC_OK : irc_host::cuda_status(e, "irc_plan_destroy");
+}
+
+int irc_plan_tc_layout(irc_plan *pl, int max_slots, int order)
+{
+    if (!pl || (max_slots != 1 && max_slots != 2 && max_slots != 4) || (order != 0 && order != 1)) {
+        irc_host::set_error("irc_plan_tc_layout: need a plan, max_slots in {1, 2, 4} and order in {0, 1}");
+        return IRC_E_INVAL;
+    }
+    const int nChunks = pl->dev.nChunks;
+    std::vector<int32_t> moff, ms, mn;
+    merge_runs(pl->h_roff, pl->h_rs, pl->h_rn, nChunks, moff, ms, mn);
+    std::vector<irc::TcItem> items = build_tc_items(pl->h_q0, pl->h_nq, moff.data(), mn.data(), nChunks, max_slots,
+                                                    order);
+    void *buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, sizeof(irc::TcItem) * (items.size() ? items.size() : 1));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(buf, items.data(), sizeof(irc::TcItem) * items.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        if (buf) cudaFree(buf);
+        return irc_host::cuda_status(e, "irc_plan_tc_layout");
+    }
+    if (pl->tc_items_buf) cudaFree(pl->tc_items_buf);   // synchronises the device: no launch still reads it
+    pl->tc_items_buf = buf;
+    pl->tc_items = reinterpret_cast<const irc::TcItem *>(buf);
+    pl->n_tc_items = (int)items.size();
+    return IRC_OK;
 }
 
 int irc_plan_check(irc_plan *pl, void *stream)
