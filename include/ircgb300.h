@@ -275,6 +275,11 @@ int irc_sort_save(const char *path, const float *rho, const float *delta, const 
 int irc_sort_load(const char *path, float *rho, float *delta, int64_t *nneigh, int64_t *ordrho, int64_t nSpk,
                   void *stream);
 
+/* out[i] = (float)in[i] for n FP16 values (device pointers; in 4-byte and out
+ * 16-byte aligned): features streamed from host memory as FP16 are widened
+ * to the FP32 the kernels read.  No reference counterpart. */
+int irc_f16_to_f32(float *out, const void *in, int64_t n, void *stream);
+
 /* The drift linkage of calc_drift_ (matlab/irc2.m:6373-6465) on the device.
  * vrAmp, vrPos [nSpk] (device): spike amplitudes and positions (second
  * column of mrPos_spk).  Chunks of equal spike counts, viLim [n+1] int64

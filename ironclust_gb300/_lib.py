@@ -52,6 +52,7 @@ SIGNATURES = {
     "irc_fet_load_site": [_P, _P, _P, _I, _P, _P, _I, _I, _P, _P, _L, _P],
     "irc_knn_save_site": [C.c_char_p, _I, _P, _I, _I, _L, _P, _L, _P],
     "irc_sort_save": [C.c_char_p, _P, _P, _P, _P, _L, _P],
+    "irc_f16_to_f32": [_P, _P, _L, _P],
     "irc_sort_load": [C.c_char_p, _P, _P, _P, _P, _L, _P],
     "irc_sort_rho": [_P, _P, _L, _P],
     "irc_assign_cluster_knn": [_P, _P, _P, _L, _P, _P, _P, _P, _P, _P, _I, _L, _F, _I, _P],

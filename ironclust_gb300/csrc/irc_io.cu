@@ -18,6 +18,10 @@
 //   sort.irc   rho (single), delta (single), nneigh (int64), ordrho
 //       (double) concatenated (sort_cache_ + struct_save_bin_,
 //       matlab/irc2.m:356-391, :1733-1750).  irc_sort_save / irc_sort_load.
+//
+// irc_f16_to_f32 widens features kept as FP16 in host memory (streamed in
+// half the bytes) after their copy to the device.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -359,4 +363,32 @@ extern "C" int irc_sort_load(const char *path, float *rho, float *delta, int64_t
     }
     cudaFreeAsync(ord, s);
     return rc;
+}
+
+namespace {
+__global__ void k_f16_to_f32(float *__restrict__ out, const __half *__restrict__ in, int64_t n)
+{
+    const int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * 4;
+    if (i0 + 3 < n) {
+        const __half2 a = *reinterpret_cast<const __half2 *>(in + i0);
+        const __half2 b = *reinterpret_cast<const __half2 *>(in + i0 + 2);
+        const float2 fa = __half22float2(a), fb = __half22float2(b);
+        *reinterpret_cast<float4 *>(out + i0) = make_float4(fa.x, fa.y, fb.x, fb.y);
+    } else {
+        for (int64_t i = i0; i < n; ++i) out[i] = __half2float(in[i]);
+    }
+}
+}  // namespace
+
+extern "C" int irc_f16_to_f32(float *out, const void *in, int64_t n, void *stream)
+{
+    if (!out || !in || n < 0 || (reinterpret_cast<uintptr_t>(in) & 3) || (reinterpret_cast<uintptr_t>(out) & 15)) {
+        irc_host::set_error("irc_f16_to_f32: null or misaligned pointer (in: 4-byte, out: 16-byte alignment)");
+        return IRC_E_INVAL;
+    }
+    if (n == 0) return IRC_OK;
+    const int64_t threads = (n + 3) / 4;
+    k_f16_to_f32<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(out, (const __half *)in, n);
+    IRC_CHECK_LAUNCH("irc_f16_to_f32");
+    return IRC_OK;
 }
