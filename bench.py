@@ -354,58 +354,39 @@ def run_batched(args, dev, torch, irc, flush, stream):
 
 def run_stream(args, dev, torch, irc):
     """The multi-day shape streamed from pinned host memory (FP16 features,
-    site groups of ~4M spikes, copies overlapped with compute on three
-    streams): end-to-end spikes/s from the first copy in to the last copy
-    out, the kernels' share, and recall / rho error against the FP64 oracle
-    on a subsample of about a million spikes (whole sites of the first
-    group)."""
+    blocks of 128 drift chunks through a five-block device ring, copies
+    overlapped with compute on three streams): end-to-end spikes/s from the
+    first copy in to the last copy out, and recall / rho error against the
+    FP64 oracle on one whole block in the middle of the recording."""
     from ironclust_gb300 import stream
     t0 = time.perf_counter()
     wl = stream.make_workload(total=args.stream_spikes)
     gen_s = time.perf_counter() - t0
     st = stream.Streamer(wl, knn=KNN, mode="bf16")
-    st.run()                                           # warm-up: operand buffers, L2
+    st.run()                                           # warm-up: plan buffers, caches
     ms = [st.run() for _ in range(2)]
-    N = int(wl["bases"][-1])
+    N = int(wl["block_base"][-1])
     h2d, d2h = st.bytes_per_pass()
     res = {"workload": "stream%dm" % round(N / 1e6), "spikes": N, "sites": len(wl["sizes"]),
-           "chunks": wl["n_chunks"], "features": wl["n_dim"], "groups": len(st.groups),
+           "chunks": wl["n_chunks"], "features": wl["n_dim"], "blocks": wl["n_blocks"],
            "pairs": int(sum(plan_pairs_of(p) for p in st.plans)), "generation_s": gen_s,
            "ms": sum(ms) / len(ms), "spikes_per_s": N / (sum(ms) / len(ms) / 1e3),
            "h2d_bytes": h2d, "d2h_bytes": d2h,
            "host_link_gbs": (h2d + d2h) / (sum(ms) / len(ms) / 1e3) / 1e9,
            "data": "synthetic: FP16 features in pinned host memory, random-walk + 0.01/step drift"}
-    # recall / rho error vs FP64 on whole sites of the first group, ~1M spikes
     from oracle import oracle as O
-    g0 = st.groups[0]
-    b0 = int(wl["bases"][g0[0]])
-    sites, n_sub = [], 0
-    for s in g0:
-        sites.append(s)
-        n_sub += int(wl["sizes"][s])
-        if n_sub >= 1_000_000:
-            break
-    hits = tot = n_bad = n_rho = 0
-    rel_max = 0.0
-    for s in sites:
-        a, z = int(wl["bases"][s]), int(wl["bases"][s + 1])
-        plan = stream.site_plan_from_members(wl["lims"][s], wl["members"], 0)
-        plan.update(q_base=0, n_out=z - a, n_f=z - a)
-        F = wl["F16"][a:z].numpy().astype(np.float32)
-        i64, d64 = O.exact_knn_f64(F, plan, KNN)
-        got = st.out["miKnn"][a:z].numpy() - (a - b0)
-        nval = np.isfinite(d64).sum(1)                 # neighbours that exist (small sites have fewer)
-        hits += sum(len(set(x[:v]) & set(y[:v])) for x, y, v in zip(got, i64, nval))
-        tot += int(nval.sum())
-        ok = np.isfinite(d64[:, KNN - 1])             # sites too small for 30 neighbours have none
-        if ok.any():
-            rho64 = 1.0 / np.sqrt(d64[ok, KNN - 1])
-            rel = np.abs(st.out["rho"][a:z].numpy()[ok] - rho64) / rho64
-            rel_max = max(rel_max, float(rel.max()))
-            n_bad += int((rel > 1e-4).sum())
-            n_rho += int(ok.sum())
-    res.update(recall_vs_fp64=hits / tot, rho_max_rel_err_vs_fp64=rel_max, rho_rel_err_above_1e4=n_bad,
-               rho_checked=n_rho, check_spikes=n_sub)
+    k = wl["n_blocks"] // 2
+    a, z = st.block_rows(k)
+    i64, d64 = O.exact_knn_f64(st.ring_rows(k), dict(st.plans[k].d), KNN)
+    got = st.out["miKnn"][a:z].numpy()
+    nval = np.isfinite(d64).sum(1)                     # neighbours that exist (small pieces have fewer)
+    hits = sum(len(set(x[:v]) & set(y[:v])) for x, y, v in zip(got, i64, nval))
+    ok = np.isfinite(d64[:, KNN - 1])
+    rho64 = 1.0 / np.sqrt(d64[ok, KNN - 1])
+    rel = np.abs(st.out["rho"][a:z].numpy()[ok] - rho64) / rho64
+    res.update(recall_vs_fp64=hits / int(nval.sum()), rho_max_rel_err_vs_fp64=float(rel.max()) if ok.any() else 0.0,
+               rho_rel_err_above_1e4=int((rel > 1e-4).sum()), rho_checked=int(ok.sum()), check_block=k,
+               check_spikes=z - a)
     st.close()
     return res
 

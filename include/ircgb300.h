@@ -183,6 +183,16 @@ int irc_plan_check(irc_plan *plan, void *stream);
  * call it outside stream capture.  No reference counterpart. */
 int irc_plan_tc_layout(irc_plan *plan, int max_slots, int order);
 
+/* Working memory of the tensor-core modes: bytes a plan needs for nC
+ * features (operand rows of all nF columns + their padded FP32 copy).  By
+ * default a plan allocates it on its first tensor-core call and keeps it;
+ * irc_plan_set_tc_buffer hands it caller-owned device memory of `bytes`
+ * instead, which several plans can share when their calls are serialised on
+ * one stream (the plans of consecutive pages, for instance).  No reference
+ * counterpart. */
+size_t irc_plan_tc_bytes(const irc_plan *plan, int nC);
+int irc_plan_set_tc_buffer(irc_plan *plan, void *buf, size_t bytes);
+
 /* kNN + rho of every query of the plan (rho_paged_site_ up to the global-id
  * mapping, matlab/irc2.m:3645-3670).
  * vrKnn [n_out]: distance of the knn-th neighbour; rho [n_out] (optional) =

@@ -40,6 +40,8 @@ SIGNATURES = {
     "irc_plan_destroy": [_P],
     "irc_plan_check": [_P, _P],
     "irc_plan_tc_layout": [_P, _I, _I],
+    "irc_plan_tc_bytes": [_P, _I],
+    "irc_plan_set_tc_buffer": [_P, _P, C.c_size_t],
     "irc_site_knn": [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_delta": [_P, _P, _I, _P, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_knn_exact_noalloc": [_P, _I, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P],
@@ -80,7 +82,8 @@ def lib():
         for name, argt in SIGNATURES.items():
             f = getattr(L, name)
             f.argtypes = argt
-            f.restype = C.c_char_p if name in ("irc_last_error", "irc_status_string") else C.c_int
+            f.restype = (C.c_char_p if name in ("irc_last_error", "irc_status_string") else
+                         C.c_size_t if name == "irc_plan_tc_bytes" else C.c_int)
         _lib = L
     return _lib
 

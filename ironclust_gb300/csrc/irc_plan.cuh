@@ -72,6 +72,7 @@ struct irc_plan {
                                            // padded FP32 rows of the re-rank, allocated lazily
     size_t tc_row_bytes;
     size_t tc_bytes;                       // allocated size of tc_buf
+    int tc_external;                       // tc_buf belongs to the caller (irc_plan_set_tc_buffer)
     int ntiles[irc::kNumTileSizes];        // host copy of tile counts
     int max_nq;                            // largest query chunk
     long long pairs;                       // (query, candidate) pairs of the plan

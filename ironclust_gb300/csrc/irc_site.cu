@@ -234,14 +234,24 @@ void merge_runs(const int32_t *roff, const int32_t *rs, const int32_t *rn, int n
 }  // namespace
 
 // Tensor-core operand rows (two [nF x row_bytes] matrices) followed by the
-// re-rank's FP32 rows padded to 16-byte multiples ([nF x fp_row_bytes]);
+// re-rank's FP32 rows padded to 16-byte multiples ([nF x fp_row_bytes]) and
+// extra_bytes of working space (256-byte aligned);
 // allocated on the first tensor-core call of a plan, grown when a call
 // needs more, kept until irc_plan_destroy.
-int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, void **fp, size_t row_bytes, size_t fp_row_bytes)
+int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, void **fp, void **extra, size_t row_bytes,
+                        size_t fp_row_bytes, size_t extra_bytes)
 {
     const size_t one = (size_t)pl->dev.nF * row_bytes;
-    const size_t need = 2 * one + (size_t)pl->dev.nF * fp_row_bytes;
-    if (!pl->tc_buf || pl->tc_bytes < need || pl->tc_row_bytes != row_bytes) {
+    const size_t fpb = ((size_t)pl->dev.nF * fp_row_bytes + 255) & ~(size_t)255;
+    const size_t need = 2 * one + fpb + extra_bytes;
+    if (pl->tc_external) {
+        if (pl->tc_bytes < need) {
+            irc_host::set_error("irc_site_knn: the shared operand buffer holds %zu bytes, %zu needed",
+                                pl->tc_bytes, need);
+            return IRC_E_INVAL;
+        }
+        pl->tc_row_bytes = row_bytes;
+    } else if (!pl->tc_buf || pl->tc_bytes < need || pl->tc_row_bytes != row_bytes) {
         if (pl->tc_buf) cudaFree(pl->tc_buf);
         pl->tc_buf = nullptr;
         pl->tc_bytes = 0;
@@ -253,6 +263,7 @@ int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, void **fp, size_t ro
     *fq = pl->tc_buf;
     *fc = (char *)pl->tc_buf + one;
     *fp = (char *)pl->tc_buf + 2 * one;
+    *extra = (char *)pl->tc_buf + 2 * one + fpb;
     return IRC_OK;
 }
 
@@ -448,11 +459,33 @@ int irc_plan_destroy(irc_plan *pl)
 {
     if (!pl) return IRC_OK;
     cudaError_t e = cudaFree(pl->dmem);
-    if (pl->tc_buf) cudaFree(pl->tc_buf);
+    if (pl->tc_buf && !pl->tc_external) cudaFree(pl->tc_buf);
     if (pl->tc_items_buf) cudaFree(pl->tc_items_buf);
     free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn);
     free(pl);
     return e == cudaSuccess ? IRC_OK : irc_host::cuda_status(e, "irc_plan_destroy");
+}
+
+size_t irc_plan_tc_bytes(const irc_plan *pl, int nC)
+{
+    if (!pl || nC < 1) return 0;
+    const size_t one = (size_t)pl->dev.nF * 128;
+    const size_t fpb = ((size_t)pl->dev.nF * (size_t)((nC + 3) / 4) * 16 + 255) & ~(size_t)255;
+    return 2 * one + fpb + (size_t)256 * 64 * 4 + 256;
+}
+
+int irc_plan_set_tc_buffer(irc_plan *pl, void *buf, size_t bytes)
+{
+    if (!pl || !buf) {
+        irc_host::set_error("irc_plan_set_tc_buffer: null plan or buffer");
+        return IRC_E_INVAL;
+    }
+    if (pl->tc_buf && !pl->tc_external) cudaFree(pl->tc_buf);
+    pl->tc_buf = buf;
+    pl->tc_bytes = bytes;
+    pl->tc_row_bytes = 0;
+    pl->tc_external = 1;
+    return IRC_OK;
 }
 
 int irc_plan_tc_layout(irc_plan *pl, int max_slots, int order)

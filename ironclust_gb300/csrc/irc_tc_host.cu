@@ -20,6 +20,40 @@
 namespace {
 
 // F (f32 [nF x nC]) -> query / candidate BF16 rows of 64.
+// Centring of the tensor-core operands.  Distances do not change when every
+// feature vector is shifted by the same reference point, but the rounding
+// error of the BF16 / FP8 contraction grows with the operands' magnitude, and
+// drift can carry features far from the origin.  The operand rows are built
+// from F - ref with ref = the column means of a strided sample of at most
+// 64K of the plan's query rows (fixed summation order, so the rows are the
+// same on every call); the exact re-rank keeps reading the unshifted
+// features.
+constexpr int kMeanBlocks = 256;
+
+__global__ void k_colsum_part(const float *__restrict__ F, int nC, int stride, int nS, float *__restrict__ part)
+{
+    __shared__ float red[4][64];
+    const int c = threadIdx.x & 63, lane_r = threadIdx.x >> 6;   // 64 columns x 4 row lanes
+    const int per = (nS + gridDim.x - 1) / gridDim.x;
+    const int k0 = blockIdx.x * per, k1 = min(nS, k0 + per);
+    float acc = 0.0f;
+    if (c < nC)
+        for (int k = k0 + lane_r; k < k1; k += 4) acc += __ldg(F + (size_t)k * stride * nC + c);
+    red[lane_r][c] = acc;
+    __syncthreads();
+    if (threadIdx.x < 64)
+        part[(size_t)blockIdx.x * 64 + c] = ((red[0][c] + red[1][c]) + red[2][c]) + red[3][c];
+}
+
+__global__ void k_colsum_final(const float *__restrict__ part, int nb, int nC, int nS, float *__restrict__ ref)
+{
+    const int c = threadIdx.x;
+    if (c >= nC) return;
+    double acc = 0.0;
+    for (int b = 0; b < nb; ++b) acc += (double)part[(size_t)b * 64 + c];
+    ref[c] = nS > 0 ? (float)(acc / (double)nS) : 0.0f;
+}
+
 // The re-rank's copy of a feature row: FP32, padded with zeros to Dp4
 // float4 (16-byte aligned rows, so candidate rows gather with 128-bit loads).
 __device__ __forceinline__ void write_padded_row(const float *__restrict__ a, int nC, int Dp4,
@@ -36,8 +70,8 @@ __device__ __forceinline__ void write_padded_row(const float *__restrict__ a, in
     }
 }
 
-__global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, uint4 *__restrict__ Fq,
-                            uint4 *__restrict__ Fc, float4 *__restrict__ Fp, int Dp4)
+__global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, const float *__restrict__ ref,
+                            uint4 *__restrict__ Fq, uint4 *__restrict__ Fc, float4 *__restrict__ Fp, int Dp4)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nF) return;
@@ -45,7 +79,7 @@ __global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, uint4 *
     write_padded_row(a, nC, Dp4, Fp + (size_t)i * Dp4);
     float na = 0.0f;
     for (int k = 0; k < nC; ++k) {
-        const float f = __bfloat162float(__float2bfloat16_rn(__ldg(a + k)));
+        const float f = __bfloat162float(__float2bfloat16_rn(__ldg(a + k) - __ldg(ref + k)));
         na = __fmaf_rn(f, f, na);
     }
     const __nv_bfloat16 h = __float2bfloat16_rn(na);
@@ -61,7 +95,7 @@ __global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, uint4 *
             const int k = j * 8 + e;
             __nv_bfloat16 vq = zero, vc = zero;
             if (k < nC) {
-                const __nv_bfloat16 bf = __float2bfloat16_rn(__ldg(a + k));
+                const __nv_bfloat16 bf = __float2bfloat16_rn(__ldg(a + k) - __ldg(ref + k));
                 vc = bf;
                 vq = __float2bfloat16_rn(-2.0f * __bfloat162float(bf));
             } else if (k < nC + 3) {
@@ -80,11 +114,12 @@ __global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, uint4 *
 }
 
 // |F| maximum (bits of a non-negative float, so integer max == float max).
-__global__ void k_absmax(const float *__restrict__ F, size_t n, unsigned *__restrict__ out)
+__global__ void k_absmax(const float *__restrict__ F, size_t n, int nC, const float *__restrict__ ref,
+                         unsigned *__restrict__ out)
 {
     unsigned m = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        m = max(m, __float_as_uint(fabsf(__ldg(F + i))));
+        m = max(m, __float_as_uint(fabsf(__ldg(F + i) - __ldg(ref + i % nC))));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
@@ -112,8 +147,9 @@ __device__ __forceinline__ float from_e4m3(unsigned char v)
 constexpr int kFp8Pieces = 6;
 __device__ __forceinline__ int piece_exp(int t) { return t < 5 ? 8 - 4 * t : -9; }
 
-__global__ void k_prep_fp8(const float *__restrict__ F, int nF, int nC, const unsigned *__restrict__ amax,
-                           uint4 *__restrict__ Fq, uint4 *__restrict__ Fc, float4 *__restrict__ Fp, int Dp4)
+__global__ void k_prep_fp8(const float *__restrict__ F, int nF, int nC, const float *__restrict__ ref,
+                           const unsigned *__restrict__ amax, uint4 *__restrict__ Fq, uint4 *__restrict__ Fc,
+                           float4 *__restrict__ Fp, int Dp4)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nF) return;
@@ -123,7 +159,7 @@ __global__ void k_prep_fp8(const float *__restrict__ F, int nF, int nC, const un
     write_padded_row(a, nC, Dp4, Fp + (size_t)i * Dp4);
     float nx = 0.0f;
     for (int k = 0; k < nC; ++k) {
-        const float x = from_e4m3(to_e4m3(sc * __ldg(a + k)));
+        const float x = from_e4m3(to_e4m3(sc * (__ldg(a + k) - __ldg(ref + k))));
         nx = __fmaf_rn(x, x, nx);
     }
     unsigned char pc[kFp8Pieces], pf[kFp8Pieces];
@@ -143,7 +179,7 @@ __global__ void k_prep_fp8(const float *__restrict__ F, int nF, int nC, const un
             const int k = j * 16 + e;
             unsigned char vq = 0, vc = 0;
             if (k < nC) {
-                const unsigned char y = to_e4m3(sc * __ldg(a + k));
+                const unsigned char y = to_e4m3(sc * (__ldg(a + k) - __ldg(ref + k)));
                 vc = y;
                 vq = to_e4m3(-2.0f * from_e4m3(y));
             } else if (k < nC + kFp8Pieces) {
@@ -202,7 +238,8 @@ int make_map(CUtensorMap *m, void *base, int rows, int box_rows, bool fp8)
 
 // Plan-owned tensor-core operand buffers (irc_site.cu) and the exact
 // fallback for queries whose candidate list overflowed (irc_exact.cu).
-int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, void **fp, size_t row_bytes, size_t fp_row_bytes);
+int irc_plan_tc_buffers(irc_plan *pl, void **fq, void **fc, void **fp, void **extra, size_t row_bytes,
+                        size_t fp_row_bytes, size_t extra_bytes);
 int irc_exact_overflow_drain(irc_plan *pl, const float *F, int nC, int knn, float *vrKnn, float *rho,
                              int32_t *miKnn, float *d2Knn, cudaStream_t s);
 
@@ -216,22 +253,32 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     }
     if (knn > irc_tc::KNN_MAX) { irc_host::set_error("irc_site_knn(BF16): knn %d > %d", knn, irc_tc::KNN_MAX); return IRC_E_INVAL; }
     const int nF = pl->dev.nF;
-    void *fq, *fc, *fp;
+    void *fq, *fc, *fp, *ex;
     const int Dp4 = (nC + 3) / 4;
-    int rc = irc_plan_tc_buffers(pl, &fq, &fc, &fp, irc_tc::KP * 2, (size_t)Dp4 * 16);
+    const size_t part_bytes = sizeof(float) * kMeanBlocks * 64;
+    int rc = irc_plan_tc_buffers(pl, &fq, &fc, &fp, &ex, irc_tc::KP * 2, (size_t)Dp4 * 16, part_bytes + 256);
+    float *part = (float *)ex;
+    float *ref = (float *)((char *)ex + part_bytes);
     if (rc != IRC_OK) return rc;
     cudaError_t e = cudaMemsetAsync(pl->scratch, 0, sizeof(int), s);       // overflow-queue count
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(BF16): memset");
+    const int nQ = pl->dev.n_out;                                     // the query rows q_base ..
+    const int stride = nQ > 65536 ? (nQ + 65535) / 65536 : 1;
+    const int nS = (nQ + stride - 1) / stride;                        // sampled: q_base + k * stride
+    k_colsum_part<<<kMeanBlocks, 256, 0, s>>>(F + (size_t)pl->dev.q_base * nC, nC, stride, nS, part);
+    k_colsum_final<<<1, 64, 0, s>>>(part, kMeanBlocks, nC, nS, ref);
+    IRC_CHECK_LAUNCH("irc_site_knn(tensor core) centre");
     if (fp8) {
         unsigned *amax = reinterpret_cast<unsigned *>(pl->scratch + 1);   // free word of the plan scratch
         e = cudaMemsetAsync(amax, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(FP8): memset");
-        k_absmax<<<152 * 4, 256, 0, s>>>(F, (size_t)nF * nC, amax);
+        k_absmax<<<152 * 4, 256, 0, s>>>(F, (size_t)nF * nC, nC, ref, amax);
         IRC_CHECK_LAUNCH("irc_site_knn(FP8) absmax");
-        k_prep_fp8<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, amax, (uint4 *)fq, (uint4 *)fc, (float4 *)fp, Dp4);
+        k_prep_fp8<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, ref, amax, (uint4 *)fq, (uint4 *)fc, (float4 *)fp,
+                                                    Dp4);
         IRC_CHECK_LAUNCH("irc_site_knn(FP8) prep");
     } else {
-        k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, (uint4 *)fq, (uint4 *)fc, (float4 *)fp, Dp4);
+        k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, ref, (uint4 *)fq, (uint4 *)fc, (float4 *)fp, Dp4);
         IRC_CHECK_LAUNCH("irc_site_knn(BF16) prep");
     }
     CUtensorMap mq, mc;

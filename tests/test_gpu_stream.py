@@ -1,6 +1,7 @@
-"""The streaming pipeline (FP16 host features, overlapped copies, group
-plans) gives the results of the same plans run directly, and the BF16 form
-keeps its recall against the FP64 oracle."""
+"""The page-streaming pipeline (FP16 host features, a five-block device ring,
+overlapped copies, kNN one block ahead of delta) gives the results of the
+same block plans run directly, and the BF16 form keeps its recall and rho
+accuracy against the FP64 oracle."""
 import numpy as np
 import pytest
 import torch
@@ -14,38 +15,76 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def streamed(gpu):
     wl = stream.make_workload(n_sites=24, total=1_500_000, n_chunks=1000)
-    st = stream.Streamer(wl, knn=30, mode="bf16", group_target=200_000)
-    st.run()                                      # first pass allocates the plans' operand buffers
+    st = stream.Streamer(wl, knn=30, mode="bf16")
+    st.run()                                      # first pass: caches, lazily made plan buffers
     ms = st.run()
     yield wl, st, ms
     st.close()
 
 
-def test_stream_matches_direct_plans(streamed):
+def _ring_for(st, k):
+    """Ring holding blocks k-2 .. k+2 in their slots: enough for the plans of
+    blocks k-1 .. k+1."""
+    F = np.zeros((st.N_SLOTS * st.slot_rows, st.wl["n_dim"]), np.float32)
+    for j in range(k - 2, k + 3):
+        if 0 <= j < st.wl["n_blocks"]:
+            a, z = st.block_rows(j)
+            F[st._slot(j):st._slot(j) + (z - a)] = st.wl["F16"][a:z].numpy()
+    return torch.from_numpy(F).cuda()
+
+
+@pytest.mark.parametrize("k", [0, 3, -1])
+def test_stream_matches_direct_plans(streamed, k):
     wl, st, ms = streamed
-    assert len(st.groups) > 3 and ms > 0
-    for g, (a, z) in enumerate(st.bounds):
-        F = torch.from_numpy(wl["F16"][a:z].numpy().astype(np.float32)).cuda()
-        r = irc.knn_rho_delta_site(st.plans[g], F, knn=30, mode="bf16")
-        assert np.array_equal(st.out["miKnn"][a:z].numpy(), r["miKnn"].cpu().numpy()), g
-        assert np.array_equal(st.out["rho"][a:z].numpy().view(np.int32), r["rho"].cpu().numpy().view(np.int32))
-        assert np.array_equal(st.out["delta"][a:z].numpy().view(np.int32), r["delta"].cpu().numpy().view(np.int32))
-        assert np.array_equal(st.out["nneigh"][a:z].numpy(), r["nneigh"].cpu().numpy())
+    nb = wl["n_blocks"]
+    k = k % nb
+    assert nb >= 6 and ms > 0
+    F = _ring_for(st, k)
+    R = torch.zeros(F.shape[0], dtype=torch.float32, device="cuda")
+    res = {}
+    for j in (k - 1, k, k + 1):
+        if 0 <= j < nb:
+            r = irc.site_knn(st.plans[j], F, 30, "bf16")
+            n = st.plans[j].n_out
+            R[st._slot(j):st._slot(j) + n] = r["rho"]
+            res[j] = r
+    delta, nneigh = irc.site_delta(st.plans[k], F, R, "bf16", knn=30, miKnn=res[k]["miKnn"], d2Knn=res[k]["d2Knn"])
+    a, z = st.block_rows(k)
+    assert np.array_equal(st.out["miKnn"][a:z].numpy(), res[k]["miKnn"].cpu().numpy())
+    assert np.array_equal(st.out["rho"][a:z].numpy().view(np.int32), res[k]["rho"].cpu().numpy().view(np.int32))
+    assert np.array_equal(st.out["delta"][a:z].numpy().view(np.int32), delta.cpu().numpy().view(np.int32))
+    assert np.array_equal(st.out["nneigh"][a:z].numpy(), nneigh.cpu().numpy())
 
 
 def test_stream_recall_vs_fp64(streamed):
     wl, st, _ = streamed
-    s = 1                                          # one site of the first group
-    b0 = int(wl["bases"][st.groups[0][0]])
-    a, z = int(wl["bases"][s]) - b0, int(wl["bases"][s + 1]) - b0
-    plan = stream.site_plan_from_members(wl["lims"][s], wl["members"], 0)
-    plan.update(q_base=0, n_out=z - a, n_f=z - a)
-    F = wl["F16"][b0 + a:b0 + z].numpy().astype(np.float32)
+    k = wl["n_blocks"] // 2
+    F = st.ring_rows(k)
+    plan = dict(st.plans[k].d)
     i64, d64 = O.exact_knn_f64(F, plan, 30)
-    got = st.out["miKnn"][b0 + a:b0 + z].numpy() - a
-    rec = np.mean([len(set(x) & set(y)) / 30.0 for x, y in zip(got, i64)])
-    assert rec >= 0.999, rec
+    a, z = st.block_rows(k)
+    got = st.out["miKnn"][a:z].numpy()
+    nval = np.isfinite(d64).sum(1)
+    hits = sum(len(set(x[:v]) & set(y[:v])) for x, y, v in zip(got, i64, nval))
+    assert hits / nval.sum() >= 0.999
     ok = np.isfinite(d64[:, 29])
     rho64 = 1.0 / np.sqrt(d64[ok, 29])
-    rel = np.abs(st.out["rho"][b0 + a:b0 + z].numpy()[ok] - rho64) / rho64
+    rel = np.abs(st.out["rho"][a:z].numpy()[ok] - rho64) / rho64
     assert rel.max() <= 1e-4, rel.max()
+
+
+def test_stream_global_rows(streamed):
+    """to_global maps ring rows back to recording rows: every neighbour of a
+    block lies in the block or its two neighbours, and the mapping inverts
+    the block layout."""
+    wl, st, _ = streamed
+    k = 2
+    a, z = st.block_rows(k)
+    g = st.to_global(k, st.out["miKnn"][a:z].numpy())
+    lo, hi = st.block_rows(k - 1)[0], st.block_rows(k + 1)[1]
+    assert ((g == 0) | ((g > lo) & (g <= hi))).all()
+    F16 = wl["F16"].numpy()
+    ring = st.ring_rows(k)
+    mi = st.out["miKnn"][a:z].numpy()
+    sel = mi[:, 0] > 0
+    assert np.array_equal(ring[mi[sel, 0] - 1], F16[g[sel, 0] - 1].astype(np.float32))

@@ -168,3 +168,45 @@ def test_fet_selection_matches_reference_reader(tmp_path):
         site_recs = np.concatenate([r[b:b + c] for r, b, c in zip(recs, before, counts)])
         assert np.array_equal(site_recs[sel], IO.load_fet_site(fs, cc, s, vi, 3, 4))
         assert np.array_equal(spikes, vi)
+
+
+def test_stream_block_plans_address_the_linked_chunks():
+    """Every block plan of the page-streaming pipeline, with its ring rows
+    mapped back to the block-major recording, queries exactly the block's
+    (site, chunk) pieces and lists the non-empty linked chunks of the same
+    site, in ascending chunk order."""
+    from ironclust_gb300 import stream
+    wl = stream.make_workload(n_sites=5, total=20000, n_chunks=300, pin=False)
+    S, Bc, nb = 5, wl["block_chunks"], wl["n_blocks"]
+    lims, seg, base = wl["lims"], wl["seg"], wl["block_base"]
+    owner = np.full((int(base[-1]), 2), -1, np.int64)              # (site, chunk) of every recording row
+    for kb in range(nb):
+        for s in range(S):
+            for c in range(kb * Bc, min((kb + 1) * Bc, wl["n_chunks"])):
+                r0 = seg[kb, s] + lims[s, c] - lims[s, kb * Bc]
+                owner[r0:r0 + lims[s, c + 1] - lims[s, c]] = (s, c)
+    assert (owner >= 0).all()
+    n_slots, slot_rows = 5, int(np.max(np.diff(base)))
+    for k in range(nb):
+        p = stream.block_plan(wl, k, slot_rows, n_slots)
+        assert p["q_base"] == (k % n_slots) * slot_rows and p["n_out"] == base[k + 1] - base[k]
+
+        def glob(r):                                                # ring row -> recording row
+            j = [j for j in (k - 1, k, k + 1) if 0 <= j < nb and (j % n_slots) * slot_rows <= r
+                 < (j % n_slots) * slot_rows + base[j + 1] - base[j]]
+            assert len(j) == 1
+            return int(base[j[0]] + r - (j[0] % n_slots) * slot_rows)
+
+        seen = 0
+        for i in range(len(p["q0"])):
+            g = glob(int(p["q0"][i]))
+            s, c = owner[g]
+            assert p["nq"][i] == lims[s, c + 1] - lims[s, c]
+            assert (owner[g:g + p["nq"][i]] == (s, c)).all()
+            want = [m for m in wl["members"][:, c] if lims[s, m + 1] > lims[s, m]]
+            runs = range(p["roff"][i], p["roff"][i + 1])
+            got = [tuple(owner[glob(int(p["rs"][r]))]) for r in runs]
+            assert got == [(s, m) for m in want]
+            assert [int(p["rn"][r]) for r in runs] == [lims[s, m + 1] - lims[s, m] for m in want]
+            seen += int(p["nq"][i])
+        assert seen == p["n_out"]
