@@ -73,6 +73,8 @@ struct irc_plan {
     size_t tc_row_bytes;
     size_t tc_bytes;                       // allocated size of tc_buf
     int tc_external;                       // tc_buf belongs to the caller (irc_plan_set_tc_buffer)
+    int n_row_iv;                          // rows of F the plan reads: n_row_iv intervals
+    int row_iv[2 * 8];                     // [lo, hi) pairs, ascending (at most 8; else one hull)
     int ntiles[irc::kNumTileSizes];        // host copy of tile counts
     int max_nq;                            // largest query chunk
     long long pairs;                       // (query, candidate) pairs of the plan

@@ -338,6 +338,31 @@ int irc_site_delta_list(irc_plan *plan, const float *F, int nC, const float *R, 
                         const int32_t *miKnn, const float *d2Knn, float *delta, int32_t *nneigh,
                         cudaStream_t s);
 
+// Rows of F a plan reads (its queries and candidate runs) as merged [lo, hi)
+// intervals; more than 8 collapse to their hull.  Operand preparation runs
+// over these rows only (a streaming ring holds rows no plan of the moment
+// reads).
+static void row_intervals(const int32_t *q0, const int32_t *nq, const int32_t *rs, const int32_t *rn, int nChunks,
+                          int nRuns, irc_plan *pl)
+{
+    std::vector<std::pair<int, int>> iv;
+    iv.reserve((size_t)nChunks + nRuns);
+    for (int i = 0; i < nChunks; ++i) iv.emplace_back(q0[i], q0[i] + nq[i]);
+    for (int r = 0; r < nRuns; ++r) iv.emplace_back(rs[r], rs[r] + rn[r]);
+    std::sort(iv.begin(), iv.end());
+    std::vector<std::pair<int, int>> m;
+    for (const auto &x : iv) {
+        if (!m.empty() && x.first <= m.back().second) m.back().second = std::max(m.back().second, x.second);
+        else m.push_back(x);
+    }
+    if (m.size() > 8) m.assign(1, std::make_pair(m.front().first, m.back().second));
+    pl->n_row_iv = (int)m.size();
+    for (size_t k = 0; k < m.size(); ++k) {
+        pl->row_iv[2 * k] = m[k].first;
+        pl->row_iv[2 * k + 1] = m[k].second;
+    }
+}
+
 extern "C" {
 
 int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const int32_t *roff,
@@ -451,6 +476,7 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     pl->dev.nRuns = (int)ms.size();
     pl->max_nq = max_nq;
     pl->pairs = pairs;
+    row_intervals(q0, nq, rs, rn, nChunks, nRuns, pl);
     *out = pl;
     return IRC_OK;
 }

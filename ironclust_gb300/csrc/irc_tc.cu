@@ -18,7 +18,8 @@
 // every tile of its slot.  Each slot's candidate tiles are streamed twice:
 //   pass 1  every thread folds its columns into 32 per-column minima (one
 //           FMNMX per pair, no branches); per query, the 64th smallest of the
-//           128 minima is an upper bound tau on the 64th nearest approximate
+//           128 minima (found by a bitwise search, rounded up by < 2^-11
+//           relative) is an upper bound tau on the 64th nearest approximate
 //           distance (64 distinct candidates lie at or below it);
 //   pass 2  every thread marks the pairs at or below tau in a 32-bit mask
 //           (one compare and one predicated OR per pair) and appends only the
@@ -57,6 +58,7 @@ constexpr uint32_t TMEM_COLS = NBUF * BN;         // all 512 columns (one CTA pe
 constexpr size_t LIST_BYTES = (size_t)LROWP * PARTS * BM * 4;
 constexpr int WARP_KEYS = 64;                     // sorted re-rank keys kept per epilogue warp
 constexpr int QROW4 = 16;                         // float4 of a staged query row (nC <= 64)
+constexpr int TAU_LOW_BIT = 12;                   // threshold search stops at this bit (2^-11 relative)
 // After the passes the tile ring (A tile + STAGES candidate tiles) is idle;
 // each epilogue warp stages its re-rank candidates' rows in one share of it.
 constexpr int STAGE_F4 = (int)(TILE_BYTES * (1 + STAGES) / EPI_WARPS / 16);
@@ -372,15 +374,37 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
 #pragma unroll
         for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
         slot_barrier(s, slot_threads);
-        for (int L = 0; L < 32 / PARTS; ++L) {
-            const int rl = part * (32 / PARTS) + L;            // row inside the quarter
-            const float *bl = qarea + rl * BROW;
-            unsigned v4[4];
+        // The warp's 8 rows at once (independent chains): a bitwise search,
+        // from the top, of the largest t with fewer than 64 minima below it,
+        // i.e. of the 64th smallest minimum, on the non-negative float bit
+        // patterns.  It stops at TAU_LOW_BIT and rounds up, so tau is an
+        // upper bound of the 64th smallest within 2^-11 of it (a few more
+        // candidates listed, never fewer).
+        constexpr int RL = 32 / PARTS;
+        unsigned v4[RL][4], ans[RL];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) v4[u] = __float_as_uint(bl[u * 32 + lane]);
-            warp_bitonic<unsigned, 4>(v4, lane);
-            const unsigned kth = __shfl_sync(0xffffffffu, v4[63 % 4], 63 / 4);
-            if (lane == 0) sTau[quarter * 32 + rl] = __uint_as_float(kth);
+        for (int L = 0; L < RL; ++L) {
+            const float *bl = qarea + (part * RL + L) * BROW;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v4[L][u] = __float_as_uint(bl[u * 32 + lane]);
+            ans[L] = 0u;
+        }
+#pragma unroll 1
+        for (int b = 30; b >= TAU_LOW_BIT; --b) {
+#pragma unroll
+            for (int L = 0; L < RL; ++L) {
+                const unsigned t = ans[L] | (1u << b);
+                const unsigned c = (unsigned)(v4[L][0] < t) + (unsigned)(v4[L][1] < t) + (unsigned)(v4[L][2] < t) +
+                                   (unsigned)(v4[L][3] < t);
+                if (__reduce_add_sync(0xffffffffu, c) < 64u) ans[L] = t;
+            }
+        }
+        if (lane < RL) {
+            unsigned a = ans[0];
+#pragma unroll
+            for (int L = 1; L < RL; ++L)
+                if (lane == L) a = ans[L];
+            sTau[quarter * 32 + part * RL + lane] = __uint_as_float(min(a | ((1u << TAU_LOW_BIT) - 1u), 0x7f800000u));
         }
         slot_barrier(s, slot_threads);     // minima rows are read; the list rows may be written
     }

@@ -54,65 +54,6 @@ __global__ void k_colsum_final(const float *__restrict__ part, int nb, int nC, i
     ref[c] = nS > 0 ? (float)(acc / (double)nS) : 0.0f;
 }
 
-// The re-rank's copy of a feature row: FP32, padded with zeros to Dp4
-// float4 (16-byte aligned rows, so candidate rows gather with 128-bit loads).
-__device__ __forceinline__ void write_padded_row(const float *__restrict__ a, int nC, int Dp4,
-                                                 float4 *__restrict__ out)
-{
-    for (int j = 0; j < Dp4; ++j) {
-        const int k = 4 * j;
-        float4 v;
-        v.x = k + 0 < nC ? __ldg(a + k + 0) : 0.0f;
-        v.y = k + 1 < nC ? __ldg(a + k + 1) : 0.0f;
-        v.z = k + 2 < nC ? __ldg(a + k + 2) : 0.0f;
-        v.w = k + 3 < nC ? __ldg(a + k + 3) : 0.0f;
-        out[j] = v;
-    }
-}
-
-__global__ void k_prep_bf16(const float *__restrict__ F, int nF, int nC, const float *__restrict__ ref,
-                            uint4 *__restrict__ Fq, uint4 *__restrict__ Fc, float4 *__restrict__ Fp, int Dp4)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nF) return;
-    const float *a = F + (size_t)i * nC;
-    write_padded_row(a, nC, Dp4, Fp + (size_t)i * Dp4);
-    float na = 0.0f;
-    for (int k = 0; k < nC; ++k) {
-        const float f = __bfloat162float(__float2bfloat16_rn(__ldg(a + k) - __ldg(ref + k)));
-        na = __fmaf_rn(f, f, na);
-    }
-    const __nv_bfloat16 h = __float2bfloat16_rn(na);
-    const float rem1 = na - __bfloat162float(h);
-    const __nv_bfloat16 m = __float2bfloat16_rn(rem1);
-    const __nv_bfloat16 l = __float2bfloat16_rn(rem1 - __bfloat162float(m));
-    const __nv_bfloat16 one = __float2bfloat16_rn(1.0f), zero = __float2bfloat16_rn(0.0f);
-#pragma unroll 1
-    for (int j = 0; j < irc_tc::KP / 8; ++j) {
-        __align__(16) __nv_bfloat16 wq[8], wc[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int k = j * 8 + e;
-            __nv_bfloat16 vq = zero, vc = zero;
-            if (k < nC) {
-                const __nv_bfloat16 bf = __float2bfloat16_rn(__ldg(a + k) - __ldg(ref + k));
-                vc = bf;
-                vq = __float2bfloat16_rn(-2.0f * __bfloat162float(bf));
-            } else if (k < nC + 3) {
-                vq = (k == nC) ? h : (k == nC + 1) ? m : l;
-                vc = one;
-            } else if (k < nC + 6) {
-                vq = one;
-                vc = (k == nC + 3) ? h : (k == nC + 4) ? m : l;
-            }
-            wq[e] = vq;
-            wc[e] = vc;
-        }
-        Fq[(size_t)i * (irc_tc::KP / 8) + j] = *reinterpret_cast<uint4 *>(wq);
-        Fc[(size_t)i * (irc_tc::KP / 8) + j] = *reinterpret_cast<uint4 *>(wc);
-    }
-}
-
 // |F| maximum (bits of a non-negative float, so integer max == float max).
 __global__ void k_absmax(const float *__restrict__ F, size_t n, int nC, const float *__restrict__ ref,
                          unsigned *__restrict__ out)
@@ -147,53 +88,139 @@ __device__ __forceinline__ float from_e4m3(unsigned char v)
 constexpr int kFp8Pieces = 6;
 __device__ __forceinline__ int piece_exp(int t) { return t < 5 ? 8 - 4 * t : -9; }
 
-__global__ void k_prep_fp8(const float *__restrict__ F, int nF, int nC, const float *__restrict__ ref,
-                           const unsigned *__restrict__ amax, uint4 *__restrict__ Fq, uint4 *__restrict__ Fc,
-                           float4 *__restrict__ Fp, int Dp4)
+// Operand preparation, one warp per 32 consecutive rows of a row interval.
+// The rows (contiguous in F) are read coalesced into shared memory with an
+// odd row stride (nC | 1 words), so lane r working on row r has no bank
+// conflicts; every lane builds its row's query and candidate operand rows
+// (BF16: above the file; FP8: above) and stages them in shared memory in
+// 16-byte pieces XOR-swizzled by row; the warp then writes its 32 rows of
+// every output -- the re-rank's FP32 rows padded to Dp4 float4 too -- with
+// contiguous stores.
+constexpr int kPrepWarps = 4;
+
+size_t prep_smem(int nC)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nF) return;
-    const float am = __uint_as_float(*amax);
-    const float sc = am > 0.0f ? 32.0f / am : 1.0f;
-    const float *a = F + (size_t)i * nC;
-    write_padded_row(a, nC, Dp4, Fp + (size_t)i * Dp4);
-    float nx = 0.0f;
-    for (int k = 0; k < nC; ++k) {
-        const float x = from_e4m3(to_e4m3(sc * (__ldg(a + k) - __ldg(ref + k))));
-        nx = __fmaf_rn(x, x, nx);
+    return (size_t)kPrepWarps * (2 * 32 * 128 + 32 * (size_t)(nC | 1) * 4) + 64 * 4;
+}
+
+template <bool FP8>
+__global__ void __launch_bounds__(32 * kPrepWarps)
+k_prep(const float *__restrict__ F, int lo, int n, int nC, const float *__restrict__ ref,
+       const unsigned *__restrict__ amax, uint4 *__restrict__ Fq, uint4 *__restrict__ Fc, float *__restrict__ Fp,
+       int Dp4)
+{
+    extern __shared__ __align__(16) unsigned char prep_sm[];
+    const int nCs = nC | 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint4 *sq = reinterpret_cast<uint4 *>(prep_sm) + (size_t)warp * 2 * 32 * 8;     // [32 rows][8], swizzled
+    uint4 *sc = sq + 32 * 8;
+    float *sref = reinterpret_cast<float *>(prep_sm + (size_t)kPrepWarps * 2 * 32 * 128);
+    float *w = sref + 64 + (size_t)warp * 32 * nCs;
+    for (int k = threadIdx.x; k < nC; k += blockDim.x) sref[k] = __ldg(ref + k);
+    __syncthreads();
+    const long long r0 = (long long)lo + ((long long)blockIdx.x * kPrepWarps + warp) * 32;
+    if (r0 >= (long long)lo + n) return;
+    const int nr = (int)min(32LL, (long long)lo + n - r0);
+    const float *src = F + (size_t)r0 * nC;
+    for (int t = lane; t < nr * nC; t += 32) {
+        const int r = t / nC;
+        w[r * nCs + (t - r * nC)] = __ldg(src + t);
     }
-    unsigned char pc[kFp8Pieces], pf[kFp8Pieces];
-    float rem = nx;
-#pragma unroll
-    for (int t = 0; t < kFp8Pieces; ++t) {
-        const float f = ldexpf(1.0f, piece_exp(t));
-        pc[t] = to_e4m3(rem / f);
-        pf[t] = to_e4m3(f);
-        rem -= from_e4m3(pc[t]) * f;
+    __syncwarp();
+    const int W = 4 * Dp4;
+    float *dst = Fp + (size_t)r0 * W;
+    for (int t = lane; t < nr * W; t += 32) {
+        const int r = t / W, c = t - r * W;
+        dst[t] = c < nC ? w[r * nCs + c] : 0.0f;
     }
-#pragma unroll 1
-    for (int j = 0; j < 128 / 16; ++j) {
-        __align__(16) unsigned char wq[16], wc[16];
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-            const int k = j * 16 + e;
-            unsigned char vq = 0, vc = 0;
-            if (k < nC) {
-                const unsigned char y = to_e4m3(sc * (__ldg(a + k) - __ldg(ref + k)));
-                vc = y;
-                vq = to_e4m3(-2.0f * from_e4m3(y));
-            } else if (k < nC + kFp8Pieces) {
-                vq = pc[k - nC];
-                vc = pf[k - nC];
-            } else if (k < nC + 2 * kFp8Pieces) {
-                vq = pf[k - nC - kFp8Pieces];
-                vc = pc[k - nC - kFp8Pieces];
+    if (lane < nr) {
+        const float *a = w + lane * nCs;
+        uint4 *oq = sq + lane * 8, *oc = sc + lane * 8;
+        const int sw = lane & 7;
+        if (!FP8) {
+            float na = 0.0f;
+            for (int k = 0; k < nC; ++k) {
+                const float f = __bfloat162float(__float2bfloat16_rn(a[k] - sref[k]));
+                na = __fmaf_rn(f, f, na);
             }
-            wq[e] = vq;
-            wc[e] = vc;
+            const __nv_bfloat16 h = __float2bfloat16_rn(na);
+            const float rem1 = na - __bfloat162float(h);
+            const __nv_bfloat16 m = __float2bfloat16_rn(rem1);
+            const __nv_bfloat16 l = __float2bfloat16_rn(rem1 - __bfloat162float(m));
+            const __nv_bfloat16 one = __float2bfloat16_rn(1.0f), zero = __float2bfloat16_rn(0.0f);
+#pragma unroll 1
+            for (int j = 0; j < irc_tc::KP / 8; ++j) {
+                __align__(16) __nv_bfloat16 wq[8], wc[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int k = j * 8 + e;
+                    __nv_bfloat16 vq = zero, vc = zero;
+                    if (k < nC) {
+                        const __nv_bfloat16 bf = __float2bfloat16_rn(a[k] - sref[k]);
+                        vc = bf;
+                        vq = __float2bfloat16_rn(-2.0f * __bfloat162float(bf));
+                    } else if (k < nC + 3) {
+                        vq = (k == nC) ? h : (k == nC + 1) ? m : l;
+                        vc = one;
+                    } else if (k < nC + 6) {
+                        vq = one;
+                        vc = (k == nC + 3) ? h : (k == nC + 4) ? m : l;
+                    }
+                    wq[e] = vq;
+                    wc[e] = vc;
+                }
+                oq[j ^ sw] = *reinterpret_cast<uint4 *>(wq);
+                oc[j ^ sw] = *reinterpret_cast<uint4 *>(wc);
+            }
+        } else {
+            const float am = __uint_as_float(*amax);
+            const float scl = am > 0.0f ? 32.0f / am : 1.0f;
+            float nx = 0.0f;
+            for (int k = 0; k < nC; ++k) {
+                const float x = from_e4m3(to_e4m3(scl * (a[k] - sref[k])));
+                nx = __fmaf_rn(x, x, nx);
+            }
+            unsigned char pc[kFp8Pieces], pf[kFp8Pieces];
+            float rem = nx;
+#pragma unroll
+            for (int t = 0; t < kFp8Pieces; ++t) {
+                const float f = ldexpf(1.0f, piece_exp(t));
+                pc[t] = to_e4m3(rem / f);
+                pf[t] = to_e4m3(f);
+                rem -= from_e4m3(pc[t]) * f;
+            }
+#pragma unroll 1
+            for (int j = 0; j < 128 / 16; ++j) {
+                __align__(16) unsigned char wq[16], wc[16];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int k = j * 16 + e;
+                    unsigned char vq = 0, vc = 0;
+                    if (k < nC) {
+                        const unsigned char y = to_e4m3(scl * (a[k] - sref[k]));
+                        vc = y;
+                        vq = to_e4m3(-2.0f * from_e4m3(y));
+                    } else if (k < nC + kFp8Pieces) {
+                        vq = pc[k - nC];
+                        vc = pf[k - nC];
+                    } else if (k < nC + 2 * kFp8Pieces) {
+                        vq = pf[k - nC - kFp8Pieces];
+                        vc = pc[k - nC - kFp8Pieces];
+                    }
+                    wq[e] = vq;
+                    wc[e] = vc;
+                }
+                oq[j ^ sw] = *reinterpret_cast<uint4 *>(wq);
+                oc[j ^ sw] = *reinterpret_cast<uint4 *>(wc);
+            }
         }
-        Fq[(size_t)i * 8 + j] = *reinterpret_cast<uint4 *>(wq);
-        Fc[(size_t)i * 8 + j] = *reinterpret_cast<uint4 *>(wc);
+    }
+    __syncwarp();
+    uint4 *gq = Fq + (size_t)r0 * 8, *gc = Fc + (size_t)r0 * 8;
+    for (int t = lane; t < nr * 8; t += 32) {
+        const int r = t >> 3, j = t & 7;
+        gq[t] = sq[r * 8 + (j ^ (r & 7))];
+        gc[t] = sc[r * 8 + (j ^ (r & 7))];
     }
 }
 
@@ -268,19 +295,28 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     k_colsum_part<<<kMeanBlocks, 256, 0, s>>>(F + (size_t)pl->dev.q_base * nC, nC, stride, nS, part);
     k_colsum_final<<<1, 64, 0, s>>>(part, kMeanBlocks, nC, nS, ref);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core) centre");
+    // operand rows for the rows the plan reads (its row intervals)
+    unsigned *amax = reinterpret_cast<unsigned *>(pl->scratch + 1);       // free word of the plan scratch
     if (fp8) {
-        unsigned *amax = reinterpret_cast<unsigned *>(pl->scratch + 1);   // free word of the plan scratch
         e = cudaMemsetAsync(amax, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(FP8): memset");
-        k_absmax<<<152 * 4, 256, 0, s>>>(F, (size_t)nF * nC, nC, ref, amax);
+        for (int v = 0; v < pl->n_row_iv; ++v) {
+            const int lo = pl->row_iv[2 * v], n = pl->row_iv[2 * v + 1] - lo;
+            k_absmax<<<152 * 4, 256, 0, s>>>(F + (size_t)lo * nC, (size_t)n * nC, nC, ref, amax);
+        }
         IRC_CHECK_LAUNCH("irc_site_knn(FP8) absmax");
-        k_prep_fp8<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, ref, amax, (uint4 *)fq, (uint4 *)fc, (float4 *)fp,
-                                                    Dp4);
-        IRC_CHECK_LAUNCH("irc_site_knn(FP8) prep");
-    } else {
-        k_prep_bf16<<<(nF + 255) / 256, 256, 0, s>>>(F, nF, nC, ref, (uint4 *)fq, (uint4 *)fc, (float4 *)fp, Dp4);
-        IRC_CHECK_LAUNCH("irc_site_knn(BF16) prep");
     }
+    const size_t psm = prep_smem(nC);
+    auto prep = fp8 ? k_prep<true> : k_prep<false>;
+    e = cudaFuncSetAttribute(prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): prep smem attribute");
+    for (int v = 0; v < pl->n_row_iv; ++v) {
+        const int lo = pl->row_iv[2 * v], n = pl->row_iv[2 * v + 1] - lo;
+        const int rows_per_block = 32 * kPrepWarps;
+        prep<<<(n + rows_per_block - 1) / rows_per_block, 32 * kPrepWarps, psm, s>>>(
+            F, lo, n, nC, ref, amax, (uint4 *)fq, (uint4 *)fc, (float *)fp, Dp4);
+    }
+    IRC_CHECK_LAUNCH("irc_site_knn(tensor core) prep");
     CUtensorMap mq, mc;
     if ((rc = make_map(&mq, fq, nF, 32, fp8)) != IRC_OK) return rc;       // 32 query rows per lane quarter
     if ((rc = make_map(&mc, fc, nF, irc_tc::BN, fp8)) != IRC_OK) return rc;
