@@ -216,10 +216,54 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const
         }
         __syncwarp();
     }
-    warp_bitonic<unsigned long long, PER>(kv, lane);
+    // ws[0 .. WARP_KEYS) <- the WARP_KEYS smallest keys, ascending.  With
+    // more than 64 keys, select first: a bitwise search (stopped at
+    // TAU_LOW_BIT, rounded up) bounds the k-th distance from above, and the
+    // keys at or below that bound plus 2^-16 relative -- the band below
+    // lies inside it -- are compacted into ws and sorted alone.  They are
+    // the first positions of the full sort, so the result is the same; if
+    // more than WARP_KEYS pass, the full sort runs.
+    bool sorted = false;
+    if (PER > 2) {
+        unsigned ans = 0;
+#pragma unroll 1
+        for (int b = 30; b >= TAU_LOW_BIT; --b) {
+            const unsigned t = ans | (1u << b);
+            unsigned c = 0;
 #pragma unroll
-    for (int i = 0; i < PER; ++i)
-        if (lane * PER + i < WARP_KEYS) ws[lane * PER + i] = kv[i];
+            for (int i = 0; i < PER; ++i) c += (unsigned)((unsigned)(kv[i] >> 32) < t);
+            if (__reduce_add_sync(0xffffffffu, c) < (unsigned)knn) ans = t;
+        }
+        const unsigned ub = ans | ((1u << TAU_LOW_BIT) - 1u);
+        const unsigned tb = ub >= 0x7f800000u ? 0x7f800000u
+                                              : __float_as_uint(__uint_as_float(ub) * (1.0f + 0x1p-16f));
+        int n = 0;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const bool pr = (unsigned)(kv[i] >> 32) <= tb;          // never an empty slot (~0)
+            const unsigned bal = __ballot_sync(0xffffffffu, pr);
+            const int pos = n + __popc(bal & ((1u << lane) - 1u));
+            if (pr && pos < WARP_KEYS) ws[pos] = kv[i];
+            n += __popc(bal);
+        }
+        __syncwarp();
+        if (n <= WARP_KEYS) {
+            unsigned long long v2[2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) v2[i] = lane * 2 + i < n ? ws[lane * 2 + i] : ~0ull;
+            __syncwarp();
+            warp_bitonic<unsigned long long, 2>(v2, lane);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) ws[lane * 2 + i] = v2[i];
+            sorted = true;
+        }
+    }
+    if (!sorted) {
+        warp_bitonic<unsigned long long, PER>(kv, lane);
+#pragma unroll
+        for (int i = 0; i < PER; ++i)
+            if (lane * PER + i < WARP_KEYS) ws[lane * PER + i] = kv[i];
+    }
     __syncwarp();
     // boundary band: keys within 16 ulps of the k-th distance, ordered by FP64
     const unsigned long long kk = ws[knn - 1];
@@ -229,9 +273,10 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const
         const float tol = vk * 0x1p-19f;
         unsigned mlo = 0xffffffffu, mhi = 0u;
 #pragma unroll
-        for (int i = 0; i < PER; ++i) {
-            const int e = lane * PER + i;
-            if (e < WARP_KEYS && kv[i] != ~0ull && fabsf(__uint_as_float((unsigned)(kv[i] >> 32)) - vk) <= tol) {
+        for (int i = 0; i < WARP_KEYS / 32; ++i) {
+            const int e = lane + 32 * i;
+            const unsigned long long k = ws[e];
+            if (k != ~0ull && fabsf(__uint_as_float((unsigned)(k >> 32)) - vk) <= tol) {
                 mlo = min(mlo, (unsigned)e);
                 mhi = max(mhi, (unsigned)e + 1u);
             }
