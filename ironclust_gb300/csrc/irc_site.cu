@@ -17,6 +17,7 @@
 #include "irc_common.cuh"
 #include "irc_plan.cuh"
 #include "irc_scan.cuh"
+#include "irc_tc.cuh"
 
 namespace {
 
@@ -497,7 +498,7 @@ size_t irc_plan_tc_bytes(const irc_plan *pl, int nC)
     if (!pl || nC < 1) return 0;
     const size_t one = (size_t)pl->dev.nF * 128;
     const size_t fpb = ((size_t)pl->dev.nF * (size_t)((nC + 3) / 4) * 16 + 255) & ~(size_t)255;
-    return 2 * one + fpb + (size_t)256 * 64 * 4 + 256;
+    return 2 * one + fpb + (size_t)256 * 64 * 4 + 256 + irc_tc::list_area_bytes(pl->dev.n_out);
 }
 
 int irc_plan_set_tc_buffer(irc_plan *pl, void *buf, size_t bytes)

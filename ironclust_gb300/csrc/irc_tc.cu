@@ -59,11 +59,7 @@ constexpr size_t LIST_BYTES = (size_t)LROWP * PARTS * BM * 4;
 constexpr int WARP_KEYS = 64;                     // sorted re-rank keys kept per epilogue warp
 constexpr int QROW4 = 16;                         // float4 of a staged query row (nC <= 64)
 constexpr int TAU_LOW_BIT = 12;                   // threshold search stops at this bit (2^-11 relative)
-// After the passes the tile ring (A tile + STAGES candidate tiles) is idle;
-// each epilogue warp stages its re-rank candidates' rows in one share of it.
-constexpr int STAGE_F4 = (int)(TILE_BYTES * (1 + STAGES) / EPI_WARPS / 16);
 constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + TILE_BYTES * (1 + STAGES) + LIST_BYTES +
-                              EPI_WARPS * WARP_KEYS * 8 + EPI_WARPS * QROW4 * 16 /*query rows*/ +
                               BM * 4 /*tau*/ + PARTS * BM * 4 /*counts*/ + 256;
 static_assert(PART == 32, "one TMEM load of 32 columns per warp and tile");
 static_assert((size_t)BROW * BM * 4 <= LIST_BYTES, "minima rows alias the list area");
@@ -132,42 +128,21 @@ __device__ __forceinline__ void emit(int e, unsigned long long key, int q, int k
     }
 }
 
-// Exact re-rank of the candidates listed for query q in its PARTS part-lists
-// (lists[p*LROWP + i], i < cnt[p]), warp-cooperative.  Requires knn <= 32.
-// 16-byte asynchronous global -> shared copy (no register round trip), and
-// the wait for this thread's outstanding copies.
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sm100::smem_u32(smem)), "l"(gmem) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_wait_all()
-{
-    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
-}
-
+// Exact re-rank of the cL candidates listed for query q (list[0 .. cL)),
+// warp-cooperative; o = q - q_base.  Requires knn <= 32.  Candidate e is
+// lane e % 32 of round e / 32, and every lane gathers its own rows.
 template <int PER>
-__device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const int (&cnt)[PARTS], int q,
+__device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL, int q,
                                        const float *__restrict__ F, const float4 *__restrict__ Fp, int Dp4,
-                                       float4 *__restrict__ qs, float4 *__restrict__ stage, int nC, int knn, size_t o,
-                                       unsigned long long *ws, int lane, int *miKnn, float *d2Knn, float *vrKnn,
-                                       float *rho)
+                                       float4 *__restrict__ qs, int nC, int knn, size_t o, unsigned long long *ws,
+                                       int lane, int *miKnn, float *d2Knn, float *vrKnn, float *rho)
 {
     const float *a = F + (size_t)q * nC;
-    int cL = 0;
-#pragma unroll
-    for (int p = 0; p < PARTS; ++p) cL += cnt[p];
     // the query row, staged once per warp (broadcast reads below)
     if (lane < Dp4) qs[lane] = __ldg(Fp + (size_t)q * Dp4 + lane);
-    // Exact FP32 distances with the reference arithmetic (d = b - a, fused
-    // accumulate in feature order).  Staged (stage != nullptr): candidate e is
-    // lane e % CB of batch e / CB; a batch's rows are copied into this warp's
-    // staging area with asynchronous 16-byte copies, all in flight at once
-    // (consecutive lanes copy consecutive pieces of the same rows), then each
-    // lane reads its candidate's row from shared memory.  Direct: candidate e
-    // is lane e % 32 of round e / 32 and every lane gathers its own rows.
-    const int CB = stage ? min(32, STAGE_F4 / Dp4) : 32;
-    const int nbatch = (cL + CB - 1) / CB;            // <= PER (checked by the caller)
+    // exact FP32 distances with the reference arithmetic (d = b - a, fused
+    // accumulate in feature order)
+    const int nbatch = (cL + 31) / 32;                // <= PER (checked by the caller)
     unsigned long long kv[PER];
 #pragma unroll
     for (int i = 0; i < PER; ++i) kv[i] = ~0ull;
@@ -175,36 +150,14 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const
 #pragma unroll
     for (int bi = 0; bi < PER; ++bi) {
         if (bi >= nbatch) break;
-        const int e = bi * CB + lane;
-        const bool has = lane < CB && e < cL;
-        int idx = q;                                  // a valid row for lanes without a candidate
-        if (has) {
-            int p = 0, r = e;
-#pragma unroll
-            for (int u = 0; u < PARTS - 1; ++u)
-                if (p == u && r >= cnt[u]) { r -= cnt[u]; p = u + 1; }
-            idx = (int)lists[p * LROWP + r];
-        }
-        const float4 *bs;
-        if (stage) {
-            const int nf = min(CB, cL - bi * CB) * Dp4; // float4 pieces of this batch
-            for (int f0 = 0; f0 < nf; f0 += 32) {         // warp-uniform trip count
-                const int f = f0 + lane;
-                const int cl = min(f / Dp4, 31), c4 = f - (f / Dp4) * Dp4;
-                const int row = __shfl_sync(0xffffffffu, idx, cl);
-                if (f < nf) cp_async16(stage + f, Fp + (size_t)row * Dp4 + c4);
-            }
-            cp_async_wait_all();
-            __syncwarp();
-            bs = stage + lane * Dp4;
-        } else {
-            bs = Fp + (size_t)idx * Dp4;
-        }
-        if (has) {
+        const int e = bi * 32 + lane;
+        if (e < cL) {
+            const int idx = (int)__ldg(list + e);
+            const float4 *bs = Fp + (size_t)idx * Dp4;
             float acc = 0.0f;
 #pragma unroll 3
             for (int c4 = 0; c4 < Dp4; ++c4) {
-                const float4 av = qs[c4], bv = bs[c4];
+                const float4 av = qs[c4], bv = __ldg(bs + c4);
                 const int c = 4 * c4;
                 acc = irc::dterm(acc, bv.x, av.x);
                 if (c + 1 < nC) acc = irc::dterm(acc, bv.y, av.y);
@@ -214,7 +167,6 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ lists, const
             if (acc > 0.0f && acc < IRC_SINGLE_INF_F)
                 kv[bi] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
         }
-        __syncwarp();
     }
     // ws[0 .. WARP_KEYS) <- the WARP_KEYS smallest keys, ascending.  With
     // more than 64 keys, select first: a bitwise search (stopped at
@@ -358,13 +310,9 @@ __device__ __forceinline__ int chunk_tiles(const irc::PlanDev &p, int chunk)
 // 32 columns `part` of every tile of its slot.  Each slot's epilogue warps
 // synchronise only among themselves (named barrier 1 + slot).
 __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::TcItem &it, const int (&nt)[4], int qps,
-                                         int bps, uint32_t tmem, uint32_t *lists, unsigned long long *wkeys,
-                                         float *sTau, int *sCnt, uint64_t *acc_full, uint64_t *acc_empty,
-                                         volatile int *abort_flag, const float *__restrict__ F,
-                                         const float4 *__restrict__ Fp, float4 *__restrict__ qrows,
-                                         float4 *__restrict__ ring, int nC, int knn,
-                                         float *vrKnn, float *rho, int *miKnn, float *d2Knn, int *scratch, int warp,
-                                         int lane)
+                                         int bps, uint32_t tmem, uint32_t *lists, float *sTau, int *sCnt,
+                                         uint64_t *acc_full, uint64_t *acc_empty, volatile int *abort_flag,
+                                         const irc_tc::ListOut &lo, int *scratch, int warp, int lane)
 {
     const int ew = warp - 2;                      // 0..15
     const int quarter = warp & 3;                 // TMEM lane quarter this warp may access
@@ -491,52 +439,69 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
     }
     sCnt[row * PARTS + part] = ovf ? -1 : cnt;
     slot_barrier(s, slot_threads);
-    // A CTA with one slot stages its re-rank candidates' rows in the tile
-    // ring: the barrier above spans all epilogue warps, so every TMA load and
-    // MMA of the CTA is complete; the ring was last written by the async
-    // proxy (TMA).  With several slots the ring may still be streaming
-    // another slot's tiles, and rows are gathered directly.
-    const bool staged = qps == 4;
-    if (staged) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    // exact re-rank: this warp serves 8 of its quarter's queries
-    unsigned long long *ws = wkeys + (size_t)ew * WARP_KEYS;
-    float4 *qs = qrows + (size_t)ew * QROW4;
-    float4 *stage = staged ? ring + (size_t)ew * STAGE_F4 : nullptr;
-    const int Dp4 = (nC + 3) / 4;
-    const int CB = staged ? min(32, STAGE_F4 / Dp4) : 32;
-    for (int L = 0; L < 32 / PARTS && ok; ++L) {
-        const int rl = part * (32 / PARTS) + L;
-        if (qrow + rl >= nq_s) break;
-        const int rowL = quarter * 32 + rl;
-        const int q = it.qs[s] + qrow + rl;
-        int c[PARTS];
+    // Hand the lists to the re-rank kernel: this warp packs 8 of its
+    // quarter's queries (query L in lane L) into one bump allocation and
+    // records (offset, length) per query; an overflowed part-list, a list
+    // longer than LIST_MAX or a full list area sends the query to the exact
+    // fallback instead.
+    if (!__all_sync(0xffffffffu, ok)) return;
+    constexpr int RL = 32 / PARTS;
+    int cL = -1;                                  // -1: no query in this lane, -2: to the fallback
+    if (lane < RL && qrow + part * RL + lane < nq_s) {
+        const int rowL = quarter * 32 + part * RL + lane;
+        int t = 0;
         bool over = false;
 #pragma unroll
-        for (int u = 0; u < PARTS; ++u) { c[u] = sCnt[rowL * PARTS + u]; over |= c[u] < 0; }
-        if (over) {                                   // finished by the exact fallback kernel
-            if (lane == 0) {
-                const int k = atomicAdd(scratch + 0, 1);
-                scratch[irc::kScratchLists + k] = q;
-            }
-            continue;
+        for (int u = 0; u < PARTS; ++u) {
+            const int c = sCnt[rowL * PARTS + u];
+            over |= c < 0;
+            t += c;
         }
-        const int cL = c[0] + c[1] + c[2] + c[3];
-        const int nbatch = (cL + CB - 1) / CB;
-        if (nbatch > 8) {                             // (wide rows, long list) also to the fallback
-            if (lane == 0) {
-                const int k = atomicAdd(scratch + 0, 1);
-                scratch[irc::kScratchLists + k] = q;
-            }
-            continue;
+        cL = (over || t > irc_tc::LIST_MAX) ? -2 : t;
+    }
+    const unsigned len = cL > 0 ? (unsigned)cL : 0u;
+    unsigned incl = len;
+#pragma unroll
+    for (int d = 1; d < RL; d <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, incl, RL - 1);
+    unsigned base = 0;
+    if (lane == 0 && total) base = atomicAdd(lo.count, total);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const bool fits = (unsigned long long)base + total <= (unsigned long long)lo.cap;
+    if (lane < RL && cL != -1) {
+        const int q = it.qs[s] + qrow + part * RL + lane;
+        if (cL == -2 || !fits) {
+            const int k = atomicAdd(scratch + 0, 1);
+            scratch[irc::kScratchLists + k] = q;
+        } else {
+            lo.qinfo[q - p.q_base] = make_int2((int)(base + incl - len), cL);
         }
+    }
+    if (!fits) return;
+#pragma unroll 1
+    for (int L = 0; L < RL; ++L) {
+        const int n = __shfl_sync(0xffffffffu, cL, L);
+        const unsigned off = base + __shfl_sync(0xffffffffu, incl - len, L);
+        if (n <= 0) continue;                     // warp-uniform
+        const int rowL = quarter * 32 + part * RL + L;
+        const int c0 = sCnt[rowL * PARTS + 0], c1 = sCnt[rowL * PARTS + 1], c2 = sCnt[rowL * PARTS + 2];
         const uint32_t *lr = lists + (size_t)rowL * PARTS * LROWP;
-        const size_t o = (size_t)(q - p.q_base);
-        if (nbatch <= 2)
-            rerank<2>(lr, c, q, F, Fp, Dp4, qs, stage, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
-        else if (nbatch <= 4)
-            rerank<4>(lr, c, q, F, Fp, Dp4, qs, stage, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
-        else
-            rerank<8>(lr, c, q, F, Fp, Dp4, qs, stage, nC, knn, o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        for (int e = lane; e < n; e += 32) {
+            int pp = 0, r = e;
+            if (r >= c0) {
+                r -= c0;
+                pp = 1;
+                if (r >= c1) {
+                    r -= c1;
+                    pp = 2;
+                    if (r >= c2) { r -= c2; pp = 3; }
+                }
+            }
+            lo.lists[off + e] = lr[pp * LROWP + r];
+        }
     }
 }
 
@@ -646,19 +611,14 @@ __device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem,
 template <bool FP8>
 __global__ void __launch_bounds__(THREADS, 1)
 k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
-              const irc_tc::TcItem *__restrict__ items, const float *__restrict__ F,
-              const float4 *__restrict__ Fp, int nC, int nk, int knn,
-              float *__restrict__ vrKnn, float *__restrict__ rho, int *__restrict__ miKnn,
-              float *__restrict__ d2Knn, int *__restrict__ scratch)
+              const irc_tc::TcItem *__restrict__ items, int nk, irc_tc::ListOut lo, int *__restrict__ scratch)
 {
     extern __shared__ unsigned char smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *sA = base;
     uint8_t *sB = base + TILE_BYTES;
     uint32_t *lists = reinterpret_cast<uint32_t *>(sB + STAGES * TILE_BYTES);        // [BM][PARTS][LROWP]
-    unsigned long long *wkeys = reinterpret_cast<unsigned long long *>(lists + (size_t)LROWP * PARTS * BM);
-    float4 *qrows = reinterpret_cast<float4 *>(wkeys + EPI_WARPS * WARP_KEYS);       // [EPI_WARPS][QROW4]
-    float *sTau = reinterpret_cast<float *>(qrows + EPI_WARPS * QROW4);              // [BM]
+    float *sTau = reinterpret_cast<float *>(lists + (size_t)LROWP * PARTS * BM);     // [BM]
     int *sCnt = reinterpret_cast<int *>(sTau + BM);                                  // [BM][PARTS], -1 = overflow
     uint64_t *bars = reinterpret_cast<uint64_t *>(sCnt + PARTS * BM);
     uint64_t *full = bars, *empty = bars + STAGES, *a_full = bars + 2 * STAGES;
@@ -704,8 +664,8 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
         }
         __syncwarp();
     } else {
-        epilogue(p, it, nt, qps, bps, tmem, lists, wkeys, sTau, sCnt, acc_full, acc_empty, abort_flag, F, Fp, qrows,
-                 reinterpret_cast<float4 *>(sA), nC, knn, vrKnn, rho, miKnn, d2Knn, scratch, warp, lane);
+        epilogue(p, it, nt, qps, bps, tmem, lists, sTau, sCnt, acc_full, acc_empty, abort_flag, lo, scratch, warp,
+                 lane);
     }
     sm100::tc_fence_before();
     __syncthreads();
@@ -716,24 +676,61 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
     if (threadIdx.x == 0 && *abort_flag) atomicExch(scratch + irc::kScratchErr, 1);
 }
 
+// Exact re-rank kernel: one warp per query of the plan, in query order (the
+// queries of a chunk share their candidate rows, which stay in L1/L2 for the
+// block's warps); queries without a list (qinfo.x < 0) belong to the exact
+// fallback or to no chunk.
+constexpr int RR_WARPS = 8;
+
+__global__ void __launch_bounds__(32 * RR_WARPS, 3)
+k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int n_out, int q_base,
+         const float *__restrict__ F, const float4 *__restrict__ Fp, int nC, int knn, float *__restrict__ vrKnn,
+         float *__restrict__ rho, int *__restrict__ miKnn, float *__restrict__ d2Knn)
+{
+    __shared__ unsigned long long wkeys[RR_WARPS * WARP_KEYS];
+    __shared__ float4 qrows[RR_WARPS * QROW4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int o = blockIdx.x * RR_WARPS + warp;
+    if (o >= n_out) return;
+    const int2 qi = __ldg(qinfo + o);
+    if (qi.x < 0) return;
+    const int Dp4 = (nC + 3) / 4;
+    const uint32_t *lst = lists + (unsigned)qi.x;
+    const int cL = qi.y, q = q_base + o;
+    unsigned long long *ws = wkeys + warp * WARP_KEYS;
+    float4 *qs = qrows + warp * QROW4;
+    if (cL <= 64)
+        rerank<2>(lst, cL, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+    else if (cL <= 128)
+        rerank<4>(lst, cL, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+    else
+        rerank<8>(lst, cL, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+}
+
 }  // namespace
 
 namespace irc_tc {
 
 int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F,
                   const float4 *Fp, int nC, int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn,
-                  cudaStream_t s)
+                  const ListOut &lo, cudaStream_t s)
 {
     auto kern = fp8 ? k_knn_tc<true> : k_knn_tc<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): smem attribute");
+    const int n_out = pl->dev.n_out;
+    e = cudaMemsetAsync(lo.qinfo, 0xff, (size_t)n_out * sizeof(int2), s);          // (-1, -1): no list
+    if (e == cudaSuccess) e = cudaMemsetAsync(lo.count, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): memset");
     // MMAs per tile: only the 32-byte K slices that hold data (nC features
     // plus 6 BF16 / 12 FP8 norm entries); the rest of each row is zero
     const int used = fp8 ? nC + 12 : 2 * (nC + 6);
     const int nk = (used + 31) / 32;
-    kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, F, Fp, nC, nk, knn, vrKnn, rho,
-                                                              miKnn, d2Knn, pl->scratch);
+    kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, nk, lo, pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
+    k_rerank<<<(n_out + RR_WARPS - 1) / RR_WARPS, 32 * RR_WARPS, 0, s>>>(lo.qinfo, lo.lists, n_out, pl->dev.q_base, F,
+                                                                         Fp, nC, knn, vrKnn, rho, miKnn, d2Knn);
+    IRC_CHECK_LAUNCH("irc_site_knn(tensor core) re-rank");
     return IRC_OK;
 }
 

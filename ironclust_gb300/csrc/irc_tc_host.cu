@@ -283,9 +283,11 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     void *fq, *fc, *fp, *ex;
     const int Dp4 = (nC + 3) / 4;
     const size_t part_bytes = sizeof(float) * kMeanBlocks * 64;
-    int rc = irc_plan_tc_buffers(pl, &fq, &fc, &fp, &ex, irc_tc::KP * 2, (size_t)Dp4 * 16, part_bytes + 256);
+    int rc = irc_plan_tc_buffers(pl, &fq, &fc, &fp, &ex, irc_tc::KP * 2, (size_t)Dp4 * 16,
+                                 part_bytes + 256 + irc_tc::list_area_bytes(pl->dev.n_out));
     float *part = (float *)ex;
     float *ref = (float *)((char *)ex + part_bytes);
+    const irc_tc::ListOut lo = irc_tc::list_area((char *)ex + part_bytes + 256, pl->dev.n_out);
     if (rc != IRC_OK) return rc;
     cudaError_t e = cudaMemsetAsync(pl->scratch, 0, sizeof(int), s);       // overflow-queue count
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(BF16): memset");
@@ -320,7 +322,7 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     CUtensorMap mq, mc;
     if ((rc = make_map(&mq, fq, nF, 32, fp8)) != IRC_OK) return rc;       // 32 query rows per lane quarter
     if ((rc = make_map(&mc, fc, nF, irc_tc::BN, fp8)) != IRC_OK) return rc;
-    rc = irc_tc::launch_knn_tc(fp8, mq, mc, pl, F, (const float4 *)fp, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
+    rc = irc_tc::launch_knn_tc(fp8, mq, mc, pl, F, (const float4 *)fp, nC, knn, vrKnn, rho, miKnn, d2Knn, lo, s);
     if (rc != IRC_OK) return rc;
     return irc_exact_overflow_drain(pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
 }

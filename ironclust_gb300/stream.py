@@ -184,7 +184,7 @@ class Streamer:
         self.f32 = torch.zeros((R, D), dtype=torch.float32, device=self.dev)
         self.rho = torch.zeros(R, dtype=torch.float32, device=self.dev)
         self.plans = [irc.Plan(block_plan(wl, k, self.slot_rows, self.N_SLOTS)) for k in range(nb)]
-        tc_bytes = lib().irc_plan_tc_bytes(self.plans[0].h, D)
+        tc_bytes = max(lib().irc_plan_tc_bytes(P.h, D) for P in self.plans)   # n_out differs per block
         self.tc = torch.empty(tc_bytes, dtype=torch.uint8, device=self.dev)
         for P in self.plans:
             check(lib().irc_plan_set_tc_buffer(P.h, _p(self.tc), C.c_size_t(tc_bytes)), "irc_plan_set_tc_buffer")
