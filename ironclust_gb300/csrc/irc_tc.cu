@@ -682,7 +682,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
 // fallback or to no chunk.
 constexpr int RR_WARPS = 8;
 
-__global__ void __launch_bounds__(32 * RR_WARPS, 3)
+__global__ void __launch_bounds__(32 * RR_WARPS, 4)
 k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int n_out, int q_base,
          const float *__restrict__ F, const float4 *__restrict__ Fp, int nC, int knn, float *__restrict__ vrKnn,
          float *__restrict__ rho, int *__restrict__ miKnn, float *__restrict__ d2Knn)
