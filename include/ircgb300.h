@@ -193,6 +193,15 @@ int irc_plan_tc_layout(irc_plan *plan, int max_slots, int order);
 size_t irc_plan_tc_bytes(const irc_plan *plan, int nC);
 int irc_plan_set_tc_buffer(irc_plan *plan, void *buf, size_t bytes);
 
+/* Kernel timing of the tensor-core modes.  Between irc_profile_begin and
+ * irc_profile_end every tensor-core irc_site_knn call (up to max_calls)
+ * records CUDA events on its stream around its filter kernel and around its
+ * re-rank kernel; irc_profile_end waits for them and returns the summed
+ * milliseconds of each and the number of calls timed.  Host-side bookkeeping
+ * only; no reference counterpart. */
+int irc_profile_begin(int max_calls);
+int irc_profile_end(float *filter_ms, float *rerank_ms, int *calls);
+
 /* kNN + rho of every query of the plan (rho_paged_site_ up to the global-id
  * mapping, matlab/irc2.m:3645-3670).
  * vrKnn [n_out]: distance of the knn-th neighbour; rho [n_out] (optional) =

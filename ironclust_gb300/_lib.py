@@ -42,6 +42,8 @@ SIGNATURES = {
     "irc_plan_tc_layout": [_P, _I, _I],
     "irc_plan_tc_bytes": [_P, _I],
     "irc_plan_set_tc_buffer": [_P, _P, C.c_size_t],
+    "irc_profile_begin": [_I],
+    "irc_profile_end": [_P, _P, _P],
     "irc_site_knn": [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_delta": [_P, _P, _I, _P, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_knn_exact_noalloc": [_P, _I, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P],

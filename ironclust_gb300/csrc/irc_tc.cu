@@ -34,6 +34,9 @@
 // is bound by the epilogue's instruction issue, not by the MMA.
 #include <cuda.h>
 
+#include <mutex>
+#include <vector>
+
 #include "irc_common.cuh"
 #include "irc_plan.cuh"
 #include "irc_sm100.cuh"
@@ -711,6 +714,20 @@ k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int
 
 namespace irc_tc {
 
+// Kernel timing (irc_profile_begin / irc_profile_end): three events per
+// tensor-core call -- before the filter, between filter and re-rank, after
+// the re-rank -- in a table created by irc_profile_begin.
+static std::mutex g_prof_mu;
+static std::vector<cudaEvent_t> g_prof_ev;
+static int g_prof_used = 0, g_prof_on = 0;
+
+static cudaEvent_t *profile_slot()
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (!g_prof_on || 3 * (g_prof_used + 1) > (int)g_prof_ev.size()) return nullptr;
+    return &g_prof_ev[3 * g_prof_used++];
+}
+
 int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F,
                   const float4 *Fp, int nC, int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn,
                   const ListOut &lo, cudaStream_t s)
@@ -726,12 +743,72 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
     // plus 6 BF16 / 12 FP8 norm entries); the rest of each row is zero
     const int used = fp8 ? nC + 12 : 2 * (nC + 6);
     const int nk = (used + 31) / 32;
+    cudaEvent_t *ev = profile_slot();
+    if (ev) cudaEventRecord(ev[0], s);
     kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, nk, lo, pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
+    if (ev) cudaEventRecord(ev[1], s);
     k_rerank<<<(n_out + RR_WARPS - 1) / RR_WARPS, 32 * RR_WARPS, 0, s>>>(lo.qinfo, lo.lists, n_out, pl->dev.q_base, F,
                                                                          Fp, nC, knn, vrKnn, rho, miKnn, d2Knn);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core) re-rank");
+    if (ev) cudaEventRecord(ev[2], s);
     return IRC_OK;
 }
 
 }  // namespace irc_tc
+
+extern "C" {
+
+int irc_profile_begin(int max_calls)
+{
+    using namespace irc_tc;
+    if (max_calls <= 0 || max_calls > 65536) {
+        irc_host::set_error("irc_profile_begin: max_calls must be in 1..65536");
+        return IRC_E_INVAL;
+    }
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (cudaEvent_t e : g_prof_ev) cudaEventDestroy(e);
+    g_prof_ev.clear();
+    for (int i = 0; i < 3 * max_calls; ++i) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) {
+            for (cudaEvent_t x : g_prof_ev) cudaEventDestroy(x);
+            g_prof_ev.clear();
+            return irc_host::cuda_status(r, "irc_profile_begin");
+        }
+        g_prof_ev.push_back(e);
+    }
+    g_prof_used = 0;
+    g_prof_on = 1;
+    return IRC_OK;
+}
+
+int irc_profile_end(float *filter_ms, float *rerank_ms, int *calls)
+{
+    using namespace irc_tc;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    float a = 0.0f, b = 0.0f;
+    for (int i = 0; i < g_prof_used; ++i) {
+        float x = 0.0f, y = 0.0f;
+        cudaError_t r = cudaEventSynchronize(g_prof_ev[3 * i + 2]);
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&x, g_prof_ev[3 * i], g_prof_ev[3 * i + 1]);
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&y, g_prof_ev[3 * i + 1], g_prof_ev[3 * i + 2]);
+        if (r != cudaSuccess) {
+            g_prof_on = 0;
+            return irc_host::cuda_status(r, "irc_profile_end");
+        }
+        a += x;
+        b += y;
+    }
+    if (filter_ms) *filter_ms = a;
+    if (rerank_ms) *rerank_ms = b;
+    if (calls) *calls = g_prof_used;
+    for (cudaEvent_t e : g_prof_ev) cudaEventDestroy(e);
+    g_prof_ev.clear();
+    g_prof_used = 0;
+    g_prof_on = 0;
+    return IRC_OK;
+}
+
+}  // extern "C"
