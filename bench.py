@@ -572,6 +572,57 @@ def cpu_baseline(site, plan, seconds=15.0, chunks=None):
             "seconds": t_used}
 
 
+def reference_gpu_kernels(site, plan, passes=2):
+    """The reference's own GPU kernels on this GB300, a same-box reference GPU
+    number: search_min_drift and search_delta_drift (PTX compiled from the
+    reference sources by oracle/build_oracle.py, launched through
+    oracle/ref_harness.cu with MATLAB's launch configuration) once per query
+    chunk, as search_knn_drift_ / search_delta_drift_ issue them
+    (matlab/irc2.m:3752-3789, :3814-3860), with MATLAB's gpuArray sort / min
+    stood in for by a stable device sort / min (torch).  Kernel and sort time
+    only: MATLAB's interpreter and gpuArray bookkeeping are not counted."""
+    import torch
+    if not torch.cuda.is_available():
+        return None
+    from oracle import oracle as O
+    try:
+        refk = O.RefKernels()
+    except Exception as e:                                   # PTX or harness missing on this box
+        return {"unavailable": str(e).splitlines()[0][:200]}
+    F = torch.from_numpy(site["F"]).cuda()
+    nF, nC = F.shape[0], F.shape[1]
+    chunks = []
+    for i in range(len(plan["q0"])):
+        r0, r1 = int(plan["roff"][i]), int(plan["roff"][i + 1])
+        chunks.append((torch.from_numpy(np.ascontiguousarray(plan["rs"][r0:r1])).cuda(),
+                       torch.from_numpy(np.ascontiguousarray(plan["rn"][r0:r1])).cuda(),
+                       [nC, nF, r1 - r0, int(plan["q0"][i]), int(plan["nq"][i])]))
+    rho = torch.empty(nF, dtype=torch.float32, device="cuda")
+
+    def one_pass():
+        for IBB, NBB, vn in chunks:
+            D, I = refk.search_min_drift(F, IBB, NBB, vn)
+            vs, _ = torch.sort(D, dim=1, stable=True)
+            rho[vn[3]:vn[3] + vn[4]] = 1.0 / vs[:, KNN - 1]
+        for IBB, NBB, vn in chunks:
+            D, I = refk.search_delta_drift(F, rho, IBB, NBB, vn)
+            torch.min(D, dim=1)
+
+    one_pass()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(passes):
+        one_pass()
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / passes
+    return {"ms_per_pass": ms, "spikes_per_s": nF / (ms / 1e3), "launches_per_pass": 2 * len(chunks),
+            "what": "reference search_min_drift + search_delta_drift PTX, one launch per chunk, MATLAB launch "
+                    "configuration; stable device sort / min standing in for MATLAB's gpuArray sort / min"}
+
+
 def run_reference(args):
     rank, world, _ = _dist_env()
     if rank != 0:
@@ -588,7 +639,8 @@ def run_reference(args):
         vals.append(cpu_baseline(site, plan, chunks=sample_chunks))
     wall = time.perf_counter() - t0
     v = sum(x["value"] for x in vals) / len(vals)
-    return {"metric": METRIC, "value": v, "unit": "spikes/s", "n_gpus": world, "steps": args.steps,
+    ref_gpu = reference_gpu_kernels(site, plan)
+    return {"reference_gpu_kernels": ref_gpu, "metric": METRIC, "value": v, "unit": "spikes/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
             "data": "synthetic (seeded Gaussian clusters + 5% noise, random-walk drift)",
