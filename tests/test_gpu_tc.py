@@ -128,3 +128,37 @@ def test_bf16_delta_vs_fp64(gpu, case):
     m = agree & found
     rel = np.abs(de[m] - ref[m]) / ref[m]
     assert rel.max() <= 1e-4
+
+
+def test_profile_times_filter_and_rerank(gpu):
+    """irc_profile_begin/end time the tensor-core filter and re-rank of every
+    tensor-core call in between, on the call's stream."""
+    import ctypes
+    from ironclust_gb300 import _lib
+    F, plan, _ = small_site(n=3000, d=24, n_chunks=5, seed=7)
+    P = irc.Plan(plan)
+    Fd = torch.from_numpy(F).to(gpu)
+    L = _lib.lib()
+    _lib.check(L.irc_profile_begin(4), "irc_profile_begin")
+    irc.site_knn(P, Fd, 30, "bf16")
+    irc.site_knn(P, Fd, 30, "bf16")
+    irc.site_knn(P, Fd, 30, "exact")                 # not a tensor-core call: not timed
+    a, b, n = ctypes.c_float(), ctypes.c_float(), ctypes.c_int()
+    _lib.check(L.irc_profile_end(ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)), "irc_profile_end")
+    assert n.value == 2 and a.value > 0 and b.value > 0
+    with pytest.raises(_lib.IrcError):
+        _lib.check(L.irc_profile_begin(0), "irc_profile_begin")
+
+
+@pytest.mark.parametrize("mode", ["bf16", "fp8"])
+def test_unreferenced_rows_do_not_matter(gpu, mode):
+    """Rows of F that the plan never reads (here NaN, past the last run) are
+    neither prepared nor scaled over; tiles that extend into them are masked,
+    so the results equal those without the rows, bit for bit."""
+    F, plan, _ = small_site(n=3000, d=24, n_chunks=5, seed=7)
+    F2 = np.concatenate([F, np.full((1000, F.shape[1]), np.nan, np.float32)])
+    plan2 = dict(plan, n_f=F2.shape[0])
+    r1 = irc.site_knn(irc.Plan(plan), torch.from_numpy(F).to(gpu), 30, mode)
+    r2 = irc.site_knn(irc.Plan(plan2), torch.from_numpy(F2).to(gpu), 30, mode)
+    assert np.array_equal(r1["miKnn"].cpu().numpy(), r2["miKnn"].cpu().numpy())
+    assert np.array_equal(r1["rho"].cpu().numpy().view(np.int32), r2["rho"].cpu().numpy().view(np.int32))
