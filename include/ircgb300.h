@@ -46,7 +46,7 @@ extern "C" {
 #define IRC_MODE_REF 0   /* bit-exact with the reference binned-minimum kernels */
 #define IRC_MODE_EXACT 1 /* true top-k, reference FP32 arithmetic, (d2, index) ties */
 #define IRC_MODE_BF16 2  /* tcgen05 BF16 distance filter + exact FP32 re-rank   */
-#define IRC_MODE_FP8 3   /* tcgen05 FP8-e4m3 filter (site-wide scale) + re-rank */
+#define IRC_MODE_FP8 3   /* tcgen05 FP8-e4m3 filter (plan-wide scale) + re-rank */
 
 int irc_version(void);                 /* 10000*major + 100*minor + patch */
 const char *irc_last_error(void);      /* message of the calling thread's last failure */
@@ -223,6 +223,36 @@ int irc_site_knn(irc_plan *plan, const float *F, int nC, int knn, int nThreads, 
 int irc_site_delta(irc_plan *plan, const float *F, int nC, const float *R, int nThreads,
                    int mode, int knn, const int32_t *miKnn, const float *d2Knn,
                    float *delta, int32_t *nneigh, void *stream);
+
+/* kNN, rho and delta of a plan in one stream-ordered call (the fused entry
+ * of the new host path; replaces the search_knn_drift_ -> rho_paged_site_ ->
+ * search_delta_drift_ -> delta_paged_site_ sequence of one page,
+ * matlab/irc2.m:3635-3726, up to the global-id mapping): irc_site_knn with
+ * 1024 bins, then irc_site_delta with 512 (the counts MATLAB sets).  R = rho
+ * of every column of F, or NULL to use the rho computed here (then the
+ * plan's queries must be all of F: q_base 0, n_out = nF).  d2Knn is needed
+ * in every mode but IRC_MODE_REF.  A batch plan (below) runs a whole probe in
+ * one call. */
+int irc_knn_rho_delta_site(irc_plan *plan, const float *F, int nC, const float *R, int knn, int mode,
+                           float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, float *delta, int32_t *nneigh,
+                           void *stream);
+
+/* Batches: the sites of a probe (processed one by one in the reference's
+ * parfor, matlab/irc2.m:3539-3561) as one plan over one feature matrix.
+ * irc_batch_plan_create concatenates per-site plans (site-local rows; per
+ * site, nChunks[s] entries of q0/nq, nChunks[s]+1 of roff starting at 0,
+ * roff_s[nChunks[s]] of rs/rn, back to back) with site s at rows
+ * row_base[s] .. row_base[s+1]-1 (row_base[0] = 0, nSites+1 entries); every
+ * row is a query.  irc_batch_stack copies the sites' device feature matrices
+ * (F_sites: host array of device pointers, site s [n_s x nC_s]) into one
+ * [row_base[nSites] x nCmax] matrix, zero-padded: a padded feature adds
+ * exactly 0 to every distance, so batch results equal per-site results bit
+ * for bit.  No reference counterpart. */
+int irc_batch_plan_create(irc_plan **out, int nSites, const int32_t *nChunks, const int64_t *row_base,
+                          const int32_t *q0, const int32_t *nq, const int32_t *roff, const int32_t *rs,
+                          const int32_t *rn);
+int irc_batch_stack(float *F, int nCmax, const float *const *F_sites, const int32_t *nC_sites,
+                    const int64_t *row_base, int nSites, void *stream);
 
 /* irc_site_knn in IRC_MODE_EXACT for callers that cannot allocate device
  * memory -- hosts whose device memory is reserved up front by their own pool

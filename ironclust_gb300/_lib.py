@@ -42,6 +42,9 @@ SIGNATURES = {
     "irc_plan_tc_layout": [_P, _I, _I],
     "irc_plan_tc_bytes": [_P, _I],
     "irc_plan_set_tc_buffer": [_P, _P, C.c_size_t],
+    "irc_knn_rho_delta_site": [_P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P],
+    "irc_batch_plan_create": [_P, _I, _P, _P, _P, _P, _P, _P, _P],
+    "irc_batch_stack": [_P, _I, _P, _P, _P, _I, _P],
     "irc_profile_begin": [_I],
     "irc_profile_end": [_P, _P, _P],
     "irc_site_knn": [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P],

@@ -30,10 +30,12 @@ class SiteBatch:
         n, dmax = int(self.bases[-1]), int(self.dims.max())
         self.F = np.zeros((n, dmax), np.float32)
         q0, nq, rs, rn, roff, site_of_chunk = [], [], [], [], [0], []
+        self.site_plans = []
         for i, s in enumerate(sites):
             b = int(self.bases[i])
             self.F[b:b + s["F"].shape[0], :s["F"].shape[1]] = s["F"]
             p = build_plan(s["viDrift"], np.ones(s["F"].shape[0], bool), s["mlDrift"])
+            self.site_plans.append(p)
             q0.append(p["q0"] + b)
             nq.append(p["nq"])
             rs.append(p["rs"] + b)
@@ -51,3 +53,39 @@ class SiteBatch:
     def split_knn(self, miKnn, i):
         """kNN rows of site i with indices local to that site (1-based)."""
         return np.asarray(miKnn)[self.site_slice(i)] - int(self.bases[i])
+
+    def c_plan(self):
+        """The batch plan built by the library from the per-site plans
+        (irc_batch_plan_create), the route of a C or MATLAB host."""
+        import ctypes as C
+
+        from . import irc
+        from ._lib import check, lib
+        cat = lambda k: np.ascontiguousarray(np.concatenate([p[k] for p in self.site_plans]), np.int32)
+        nch = np.array([len(p["q0"]) for p in self.site_plans], np.int32)
+        arrs = [nch, np.ascontiguousarray(self.bases, np.int64), cat("q0"), cat("nq"), cat("roff"), cat("rs"),
+                cat("rn")]
+        h = C.c_void_p()
+        check(lib().irc_batch_plan_create(C.byref(h), self.n_sites, *[a.ctypes.data_as(C.c_void_p) for a in arrs]),
+              "irc_batch_plan_create")
+        return irc.Plan.from_handle(h, self.plan)
+
+    def stack_device(self, F_sites):
+        """The stacked feature matrix from per-site device tensors
+        (irc_batch_stack): [n, max D] float32, zero-padded."""
+        import ctypes as C
+
+        import torch
+
+        from ._lib import check, lib
+        dev = F_sites[0].device
+        n, dmax = int(self.bases[-1]), int(self.dims.max())
+        out = torch.empty((n, dmax), dtype=torch.float32, device=dev)
+        ptrs = (C.c_void_p * self.n_sites)(*[t.data_ptr() for t in F_sites])
+        nc = np.ascontiguousarray(self.dims, np.int32)
+        rb = np.ascontiguousarray(self.bases, np.int64)
+        check(lib().irc_batch_stack(C.c_void_p(out.data_ptr()), dmax, C.cast(ptrs, C.c_void_p),
+                                    nc.ctypes.data_as(C.c_void_p), rb.ctypes.data_as(C.c_void_p), self.n_sites,
+                                    C.c_void_p(torch.cuda.current_stream().cuda_stream)), "irc_batch_stack")
+        return out
+

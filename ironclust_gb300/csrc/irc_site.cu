@@ -615,4 +615,115 @@ int irc_site_delta(irc_plan *pl, const float *F, int nC, const float *R, int nTh
     return IRC_E_INVAL;
 }
 
+// kNN, rho and delta of a plan in one call: irc_site_knn with the 1024 bins
+// of search_knn_drift_ and irc_site_delta with the 512 of
+// search_delta_drift_ (the counts MATLAB sets, matlab/irc2.m:3755, :3819;
+// only the REF mode depends on them), stream-ordered.  R = rho of every
+// column of F; NULL uses the rho computed here, which needs a plan whose
+// queries are all of F.
+int irc_knn_rho_delta_site(irc_plan *pl, const float *F, int nC, const float *R, int knn, int mode,
+                           float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn, float *delta, int32_t *nneigh,
+                           void *stream)
+{
+    if (!pl || !rho) { irc_host::set_error("irc_knn_rho_delta_site: null plan or rho"); return IRC_E_INVAL; }
+    if (!R && (pl->dev.q_base != 0 || pl->dev.n_out != pl->dev.nF)) {
+        irc_host::set_error("irc_knn_rho_delta_site: R is required when the plan's queries are not all of F "
+                            "(q_base %d, n_out %d, nF %d)", pl->dev.q_base, pl->dev.n_out, pl->dev.nF);
+        return IRC_E_INVAL;
+    }
+    int rc = irc_site_knn(pl, F, nC, knn, 1024, mode, vrKnn, rho, miKnn, d2Knn, stream);
+    if (rc != IRC_OK) return rc;
+    return irc_site_delta(pl, F, nC, R ? R : rho, 512, mode, knn, miKnn, d2Knn, delta, nneigh, stream);
+}
+
+// One plan for a batch of sites stacked row-wise (site s at rows
+// row_base[s] .. row_base[s+1]-1 of one feature matrix): the sites' plans
+// (site-local rows) are concatenated with their rows offset, q_base 0 and
+// every row a query.  Per-site arrays are given back to back: q0/nq hold
+// nChunks[s] entries per site, roff nChunks[s]+1 (site-local, from 0), rs/rn
+// roff_s[nChunks[s]] entries.  Candidate runs must stay inside their site.
+int irc_batch_plan_create(irc_plan **out, int nSites, const int32_t *nChunks, const int64_t *row_base,
+                          const int32_t *q0, const int32_t *nq, const int32_t *roff, const int32_t *rs,
+                          const int32_t *rn)
+{
+    if (!out || nSites <= 0 || !nChunks || !row_base || !q0 || !nq || !roff || !rs || !rn) {
+        irc_host::set_error("irc_batch_plan_create: null pointer or no site");
+        return IRC_E_INVAL;
+    }
+    *out = nullptr;
+    if (row_base[0] != 0 || row_base[nSites] > INT32_MAX) {
+        irc_host::set_error("irc_batch_plan_create: row_base must start at 0 and end below 2^31");
+        return IRC_E_INVAL;
+    }
+    std::vector<int32_t> Q0, NQ, ROFF(1, 0), RS, RN;
+    size_t c0 = 0, f0 = 0, r0 = 0;
+    for (int st = 0; st < nSites; ++st) {
+        const int64_t base = row_base[st], n = row_base[st + 1] - row_base[st];
+        const int nc = nChunks[st];
+        if (n < 0 || nc < 0) { irc_host::set_error("irc_batch_plan_create: site %d: bad sizes", st); return IRC_E_INVAL; }
+        const int32_t *ro = roff + f0;
+        if (ro[0] != 0) { irc_host::set_error("irc_batch_plan_create: site %d: roff must start at 0", st); return IRC_E_INVAL; }
+        for (int i = 0; i < nc; ++i) {
+            const int32_t a = q0[c0 + i], m = nq[c0 + i];
+            if (a < 0 || m <= 0 || a + (int64_t)m > n || ro[i + 1] < ro[i]) {
+                irc_host::set_error("irc_batch_plan_create: site %d chunk %d out of range", st, i);
+                return IRC_E_INVAL;
+            }
+            Q0.push_back((int32_t)(a + base));
+            NQ.push_back(m);
+            for (int r = ro[i]; r < ro[i + 1]; ++r) {
+                const int32_t b = rs[r0 + r], k = rn[r0 + r];
+                if (b < 0 || k <= 0 || b + (int64_t)k > n) {
+                    irc_host::set_error("irc_batch_plan_create: site %d run %d leaves its site", st, r);
+                    return IRC_E_INVAL;
+                }
+                RS.push_back((int32_t)(b + base));
+                RN.push_back(k);
+            }
+            ROFF.push_back((int32_t)RS.size());
+        }
+        c0 += nc;
+        f0 += nc + 1;
+        r0 += ro[nc];
+    }
+    const int nRows = (int)row_base[nSites];
+    return irc_plan_create(out, Q0.data(), NQ.data(), ROFF.data(), RS.data(), RN.data(), (int)Q0.size(), 0, nRows,
+                           nRows);
+}
+
+// Site feature matrices (device, site s [n_s x nC_s] row-major) stacked into
+// one [row_base[nSites] x nCmax] matrix zero-padded to nCmax columns: a
+// padded feature adds exactly 0 to every fused accumulate, so results on the
+// stack equal the per-site results bit for bit.  F_sites is a host array of
+// device pointers.
+int irc_batch_stack(float *F, int nCmax, const float *const *F_sites, const int32_t *nC_sites, const int64_t *row_base,
+                    int nSites, void *stream)
+{
+    if (!F || !F_sites || !nC_sites || !row_base || nSites <= 0 || nCmax <= 0) {
+        irc_host::set_error("irc_batch_stack: null pointer or empty batch");
+        return IRC_E_INVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t pitch = (size_t)nCmax * sizeof(float);
+    for (int st = 0; st < nSites; ++st) {
+        const int64_t n = row_base[st + 1] - row_base[st];
+        const int nc = nC_sites[st];
+        if (n < 0 || nc < 0 || nc > nCmax || (n > 0 && nc > 0 && !F_sites[st])) {
+            irc_host::set_error("irc_batch_stack: site %d: bad size or pointer", st);
+            return IRC_E_INVAL;
+        }
+        if (n == 0) continue;
+        float *dst = F + (size_t)row_base[st] * nCmax;
+        cudaError_t e = cudaSuccess;
+        if (nc > 0)
+            e = cudaMemcpy2DAsync(dst, pitch, F_sites[st], (size_t)nc * sizeof(float), (size_t)nc * sizeof(float),
+                                  (size_t)n, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess && nc < nCmax)
+            e = cudaMemset2DAsync(dst + nc, pitch, 0, (size_t)(nCmax - nc) * sizeof(float), (size_t)n, s);
+        if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_batch_stack");
+    }
+    return IRC_OK;
+}
+
 }  // extern "C"
+

@@ -281,6 +281,14 @@ class Plan:
     def from_drift(cls, viDrift_out, vl_in, mlDrift):
         return cls(build_plan(viDrift_out, vl_in, mlDrift))
 
+    @classmethod
+    def from_handle(cls, handle, plan):
+        """Wrap a plan the library created (irc_batch_plan_create); plan = its
+        arrays as a dict, for host-side use."""
+        self = cls.__new__(cls)
+        self.d, self.h, self._keep = plan, handle, []
+        return self
+
     @property
     def n_out(self):
         return int(self.d["n_out"])
@@ -326,14 +334,28 @@ def site_delta(plan, F, R, mode="ref", nThreads=512, knn=30, miKnn=None, d2Knn=N
 
 
 def knn_rho_delta_site(plan, F, knn=30, mode="ref", nThreads_rho=1024, nThreads_delta=512):
-    """One single-page site end to end: kNN, rho = 1/d_knn, delta, nneigh.
+    """One single-page site (or a batch plan) end to end: kNN, rho = 1/d_knn,
+    delta, nneigh -- one irc_knn_rho_delta_site call with MATLAB's bin counts.
     Requires every column of F to be a query (the plan covers all of F)."""
     if plan.n_out != F.shape[0] or int(plan.d["q_base"]) != 0:
         raise ValueError("knn_rho_delta_site: the plan must cover every column of F")
-    k = site_knn(plan, F, knn, mode, nThreads_rho)
-    delta, nneigh = site_delta(plan, F, k["rho"], mode, nThreads_delta, knn, k["miKnn"], k["d2Knn"])
-    k.update(delta=delta, nneigh=nneigh)
-    return k
+    if (nThreads_rho, nThreads_delta) != (1024, 512):
+        k = site_knn(plan, F, knn, mode, nThreads_rho)
+        delta, nneigh = site_delta(plan, F, k["rho"], mode, nThreads_delta, knn, k["miKnn"], k["d2Knn"])
+        k.update(delta=delta, nneigh=nneigh)
+        return k
+    n, dev = plan.n_out, F.device
+    m = _mode(mode)
+    out = dict(vrKnn=torch.empty(n, dtype=torch.float32, device=dev),
+               rho=torch.empty(n, dtype=torch.float32, device=dev),
+               miKnn=torch.empty((n, knn), dtype=torch.int32, device=dev),
+               d2Knn=torch.empty((n, knn), dtype=torch.float32, device=dev) if m != _lib.MODE_REF else None,
+               delta=torch.empty(n, dtype=torch.float32, device=dev),
+               nneigh=torch.empty(n, dtype=torch.int32, device=dev))
+    check(lib().irc_knn_rho_delta_site(plan.h, _p(F), F.shape[1], None, knn, m, _p(out["vrKnn"]), _p(out["rho"]),
+                                       _p(out["miKnn"]), _p(out["d2Knn"]), _p(out["delta"]), _p(out["nneigh"]),
+                                       _stream()), "irc_knn_rho_delta_site")
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -24,6 +24,8 @@
  *   F      = ircgb300_mex('fet_load_site',      csFiles_fet, vnSpkBefore, vnSpkSite, dimm_fet, mlPc [, viSel])
  *            ircgb300_mex('knn_save_site',      vcFile_knn, fAppend, miKnn, viSpk_out, knn)
  *            ircgb300_mex('sort_save',          vcFile, rho, delta, nneigh, ordrho)
+ *   [vrKnn, rho, miKnn, delta, nneigh] =
+ *            ircgb300_mex('knn_rho_delta_site', F, q0, nq, roff, rs, rn, q_base, n_out, knn, mode [, R])
  *   v      = ircgb300_mex('version')
  *
  * sort_rho replaces `vrRho = vrRho / max(vrRho); [~, ordrho] = sort(vrRho,
@@ -34,6 +36,14 @@
  * is; pass int64(ordrho) and the kNN lists the path kept on the device
  * instead of the _knn_<site>.irc files), icl and vnSpk_clu come back on the
  * host.
+ *
+ * knn_rho_delta_site runs one page of a site (or a batch of sites) through
+ * irc_plan_create + irc_knn_rho_delta_site + irc_plan_destroy: F is the
+ * single [nC x nF] gpuArray, the plan arrays are host int32 vectors with
+ * 0-based rows (the run selection of search_knn_drift_, as
+ * ironclust_gb300/drift.py:build_plan builds it), mode 0 REF, 1 EXACT,
+ * 2 BF16, 3 FP8; R (optional, single [nF]) is the rho of every column when
+ * the queries are not all of F.  miKnn / nneigh are 1-based into F.
  *
  * Array arguments are gpuArrays (single / int32 as the reference kernels
  * take them); vnConst may be a host or a gpuArray int32 vector (it is read on
@@ -310,6 +320,53 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         mxFree(path);
         mxGPUDestroyGPUArray(R); mxGPUDestroyGPUArray(D); mxGPUDestroyGPUArray(NN); mxGPUDestroyGPUArray(O);
         if (rc != IRC_OK) fail(rc, cmd);
+        return;
+    }
+    if (!strcmp(cmd, "knn_rho_delta_site")) {
+        if (nrhs < 11) mexErrMsgTxt("knn_rho_delta_site: F, q0, nq, roff, rs, rn, q_base, n_out, knn, mode [, R]");
+        const mxGPUArray *F = gin(prhs[1]);
+        const mwSize *fd = mxGPUGetDimensions(F);
+        const int nC = (int)fd[0], nF = (int)(mxGPUGetNumberOfElements(F) / (fd[0] ? fd[0] : 1));
+        mxFree((void *)fd);
+        const int nCh = (int)mxGetNumberOfElements(prhs[2]);
+        const int nRuns = (int)mxGetNumberOfElements(prhs[5]);
+        if ((int)mxGetNumberOfElements(prhs[3]) != nCh || (int)mxGetNumberOfElements(prhs[4]) != nCh + 1 ||
+            (int)mxGetNumberOfElements(prhs[6]) != nRuns)
+            mexErrMsgIdAndTxt("ircgb300:shape", "knn_rho_delta_site: plan array sizes disagree");
+        int32_t *q0 = (int32_t *)mxMalloc(sizeof(int32_t) * nCh), *nq = (int32_t *)mxMalloc(sizeof(int32_t) * nCh),
+                *roff = (int32_t *)mxMalloc(sizeof(int32_t) * (nCh + 1)),
+                *rs = (int32_t *)mxMalloc(sizeof(int32_t) * nRuns), *rn = (int32_t *)mxMalloc(sizeof(int32_t) * nRuns);
+        host_i32(prhs[2], q0, nCh); host_i32(prhs[3], nq, nCh); host_i32(prhs[4], roff, nCh + 1);
+        host_i32(prhs[5], rs, nRuns); host_i32(prhs[6], rn, nRuns);
+        const int q_base = (int)mxGetScalar(prhs[7]), n_out = (int)mxGetScalar(prhs[8]);
+        const int knn = (int)mxGetScalar(prhs[9]), mode = (int)mxGetScalar(prhs[10]);
+        const mxGPUArray *R = nrhs > 11 ? gin(prhs[11]) : NULL;
+        irc_plan *plan = NULL;
+        rc = irc_plan_create(&plan, q0, nq, roff, rs, rn, nCh, q_base, n_out, nF);
+        mxFree(q0); mxFree(nq); mxFree(roff); mxFree(rs); mxFree(rn);
+        if (rc != IRC_OK) fail(rc, cmd);
+        mxGPUArray *vr = gout(n_out, 1, mxSINGLE_CLASS), *rho = gout(n_out, 1, mxSINGLE_CLASS),
+                   *mi = gout(knn, n_out, mxINT32_CLASS), *de = gout(n_out, 1, mxSINGLE_CLASS),
+                   *nn = gout(n_out, 1, mxINT32_CLASS);
+        mxGPUArray *d2 = mode != IRC_MODE_REF ? gout(knn, n_out, mxSINGLE_CLASS) : NULL;
+        rc = irc_knn_rho_delta_site(plan, (const float *)mxGPUGetDataReadOnly(F), nC,
+                                    R ? (const float *)mxGPUGetDataReadOnly(R) : NULL, knn, mode,
+                                    (float *)mxGPUGetData(vr), (float *)mxGPUGetData(rho), (int32_t *)mxGPUGetData(mi),
+                                    d2 ? (float *)mxGPUGetData(d2) : NULL, (float *)mxGPUGetData(de),
+                                    (int32_t *)mxGPUGetData(nn), NULL);
+        if (rc == IRC_OK) rc = irc_plan_check(plan, NULL);
+        irc_plan_destroy(plan);
+        if (rc != IRC_OK) fail(rc, cmd);
+        plhs[0] = mxGPUCreateMxArrayOnGPU(vr);
+        if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(rho);
+        if (nlhs > 2) plhs[2] = mxGPUCreateMxArrayOnGPU(mi);
+        if (nlhs > 3) plhs[3] = mxGPUCreateMxArrayOnGPU(de);
+        if (nlhs > 4) plhs[4] = mxGPUCreateMxArrayOnGPU(nn);
+        mxGPUDestroyGPUArray(vr); mxGPUDestroyGPUArray(rho); mxGPUDestroyGPUArray(mi);
+        mxGPUDestroyGPUArray(de); mxGPUDestroyGPUArray(nn);
+        if (d2) mxGPUDestroyGPUArray(d2);
+        if (R) mxGPUDestroyGPUArray(R);
+        mxGPUDestroyGPUArray(F);
         return;
     }
     if (!strcmp(cmd, "sort_rho")) {

@@ -60,3 +60,66 @@ def test_batch_plan_packs_small_chunks(sites):
     assert b.F.shape == (sum(s["F"].shape[0] for s in sites), 33)
     # padding columns are zero
     assert not b.F[b.site_slice(0), 18:].any()
+
+
+@pytest.mark.parametrize("mode", ["ref", "bf16"])
+def test_c_batch_plan_and_stack_equal_the_host_batch(gpu, sites, mode):
+    """irc_batch_plan_create + irc_batch_stack (the route of a C or MATLAB
+    host) build the same batch as the host code: same stacked matrix, same
+    results through irc_knn_rho_delta_site, bit for bit."""
+    b = batch.SiteBatch(sites)
+    Fs = b.stack_device([torch.from_numpy(s["F"]).to(gpu) for s in sites])
+    assert np.array_equal(Fs.cpu().numpy(), b.F)
+    Pc, Ph = b.c_plan(), irc.Plan(b.plan)
+    r1 = irc.knn_rho_delta_site(Pc, Fs, knn=30, mode=mode)
+    r2 = irc.knn_rho_delta_site(Ph, torch.from_numpy(b.F).to(gpu), knn=30, mode=mode)
+    for k in ("miKnn", "nneigh"):
+        assert np.array_equal(r1[k].cpu().numpy(), r2[k].cpu().numpy()), k
+    for k in ("rho", "delta"):
+        assert np.array_equal(r1[k].cpu().numpy().view(np.int32), r2[k].cpu().numpy().view(np.int32)), k
+
+
+def test_fused_entry_with_external_rho_and_errors(gpu, sites):
+    """irc_knn_rho_delta_site with R given equals the two-call sequence with
+    the same R; without R a plan whose queries are not all of F is refused."""
+    import ctypes as C
+    from ironclust_gb300 import _lib
+    site = sites[2]
+    plan = synth.site_plan(site)
+    P = irc.Plan(plan)
+    F = torch.from_numpy(site["F"]).to(gpu)
+    k = irc.site_knn(P, F, 30, "exact")
+    R = (k["rho"] * 0.5).contiguous()                 # any rho of every column
+    d1, n1 = irc.site_delta(P, F, R, "exact", 512, 30, k["miKnn"], k["d2Knn"])
+    n = P.n_out
+    out = [torch.empty(n, dtype=torch.float32, device=gpu), torch.empty(n, dtype=torch.float32, device=gpu),
+           torch.empty((n, 30), dtype=torch.int32, device=gpu), torch.empty((n, 30), dtype=torch.float32, device=gpu),
+           torch.empty(n, dtype=torch.float32, device=gpu), torch.empty(n, dtype=torch.int32, device=gpu)]
+    p = lambda t: C.c_void_p(t.data_ptr())
+    L = _lib.lib()
+    _lib.check(L.irc_knn_rho_delta_site(P.h, p(F), F.shape[1], p(R), 30, _lib.MODES["exact"], *[p(t) for t in out],
+                                        irc._stream()), "irc_knn_rho_delta_site")
+    assert np.array_equal(out[4].cpu().numpy().view(np.int32), d1.cpu().numpy().view(np.int32))
+    assert np.array_equal(out[5].cpu().numpy(), n1.cpu().numpy())
+    sub = dict(plan, n_f=F.shape[0] + 10)               # queries no longer all of F
+    F2 = torch.cat([F, torch.zeros((10, F.shape[1]), device=gpu)])
+    P2 = irc.Plan(sub)
+    with pytest.raises(_lib.IrcError):
+        _lib.check(L.irc_knn_rho_delta_site(P2.h, p(F2), F.shape[1], None, 30, _lib.MODES["exact"],
+                                            *[p(t) for t in out], irc._stream()), "irc_knn_rho_delta_site")
+
+
+def test_c_batch_plan_rejects_a_run_leaving_its_site(gpu, sites):
+    import ctypes as C
+    from ironclust_gb300 import _lib
+    b = batch.SiteBatch(sites[:2])
+    ps = b.site_plans
+    rs = [p["rs"].copy() for p in ps]
+    rs[0][-1] = int(b.sizes[0])                         # starts past the end of site 0
+    cat = lambda parts: np.ascontiguousarray(np.concatenate(parts), np.int32)
+    arrs = [np.array([len(p["q0"]) for p in ps], np.int32), np.ascontiguousarray(b.bases, np.int64),
+            cat([p["q0"] for p in ps]), cat([p["nq"] for p in ps]), cat([p["roff"] for p in ps]), cat(rs),
+            cat([p["rn"] for p in ps])]
+    h = C.c_void_p()
+    rc = _lib.lib().irc_batch_plan_create(C.byref(h), 2, *[a.ctypes.data_as(C.c_void_p) for a in arrs])
+    assert rc != 0 and not h.value
