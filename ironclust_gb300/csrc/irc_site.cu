@@ -497,7 +497,7 @@ size_t irc_plan_tc_bytes(const irc_plan *pl, int nC)
 {
     if (!pl || nC < 1) return 0;
     const size_t one = (size_t)pl->dev.nF * 128;
-    const size_t fpb = ((size_t)pl->dev.nF * (size_t)((nC + 3) / 4) * 16 + 255) & ~(size_t)255;
+    const size_t fpb = ((size_t)pl->dev.nF * (size_t)irc_tc::fp_row4(nC) * 16 + 255) & ~(size_t)255;
     return 2 * one + fpb + (size_t)256 * 64 * 4 + 256 + irc_tc::list_area_bytes(pl->dev.n_out);
 }
 

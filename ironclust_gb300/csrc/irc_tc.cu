@@ -131,6 +131,14 @@ __device__ __forceinline__ void emit(int e, unsigned long long key, int q, int k
     }
 }
 
+// 256-bit read-only load of 8 floats (32-byte aligned).
+__device__ __forceinline__ void ld_nc_v8(const float *p, float (&v)[8])
+{
+    asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+                 : "l"(p));
+}
+
 // Exact re-rank of the cL candidates listed for query q (list[0 .. cL)),
 // warp-cooperative; o = q - q_base.  Requires knn <= 32.  Candidate e is
 // lane e % 32 of round e / 32, and every lane gathers its own rows.
@@ -156,16 +164,20 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
         const int e = bi * 32 + lane;
         if (e < cL) {
             const int idx = (int)__ldg(list + e);
-            const float4 *bs = Fp + (size_t)idx * Dp4;
+            // whole 32-byte sectors: rows are padded to a multiple of 8 floats
+            const float *bs = reinterpret_cast<const float *>(Fp + (size_t)idx * Dp4);
             float acc = 0.0f;
-#pragma unroll 3
-            for (int c4 = 0; c4 < Dp4; ++c4) {
-                const float4 av = qs[c4], bv = __ldg(bs + c4);
-                const int c = 4 * c4;
-                acc = irc::dterm(acc, bv.x, av.x);
-                if (c + 1 < nC) acc = irc::dterm(acc, bv.y, av.y);
-                if (c + 2 < nC) acc = irc::dterm(acc, bv.z, av.z);
-                if (c + 3 < nC) acc = irc::dterm(acc, bv.w, av.w);
+#pragma unroll 2
+            for (int c8 = 0; c8 < Dp4 / 2; ++c8) {
+                float bv[8];
+                ld_nc_v8(bs + 8 * c8, bv);
+                const float4 a0 = qs[2 * c8], a1 = qs[2 * c8 + 1];
+                const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                const int c = 8 * c8;
+                acc = irc::dterm(acc, bv[0], av[0]);
+#pragma unroll
+                for (int u = 1; u < 8; ++u)
+                    if (c + u < nC) acc = irc::dterm(acc, bv[u], av[u]);
             }
             if (acc > 0.0f && acc < IRC_SINGLE_INF_F)
                 kv[bi] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
@@ -697,7 +709,7 @@ k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int
     if (o >= n_out) return;
     const int2 qi = __ldg(qinfo + o);
     if (qi.x < 0) return;
-    const int Dp4 = (nC + 3) / 4;
+    const int Dp4 = irc_tc::fp_row4(nC);
     const uint32_t *lst = lists + (unsigned)qi.x;
     const int cL = qi.y, q = q_base + o;
     unsigned long long *ws = wkeys + warp * WARP_KEYS;

@@ -14,6 +14,11 @@ constexpr int LIST_MAX = 256;    // longest candidate list re-ranked (else: the 
 constexpr int LIST_AVG = 128;    // list area per plan: LIST_AVG entries per query
 using TcItem = irc::TcItem;
 
+// The re-rank's FP32 copy of a feature row, zero-padded to a multiple of 8
+// floats (32 bytes) so that it is read with whole-sector 256-bit loads:
+// width in float4.
+inline __host__ __device__ int fp_row4(int nC) { return 2 * ((nC + 7) / 8); }
+
 // Candidate lists handed from the filter kernel to the re-rank kernel:
 // qinfo[o] = (offset into lists, length) of query q_base + o, or (-1, -1);
 // lists packed by a bump allocator (count) of cap entries.

@@ -281,7 +281,7 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     if (knn > irc_tc::KNN_MAX) { irc_host::set_error("irc_site_knn(BF16): knn %d > %d", knn, irc_tc::KNN_MAX); return IRC_E_INVAL; }
     const int nF = pl->dev.nF;
     void *fq, *fc, *fp, *ex;
-    const int Dp4 = (nC + 3) / 4;
+    const int Dp4 = irc_tc::fp_row4(nC);                               // padded FP32 row, float4
     const size_t part_bytes = sizeof(float) * kMeanBlocks * 64;
     int rc = irc_plan_tc_buffers(pl, &fq, &fc, &fp, &ex, irc_tc::KP * 2, (size_t)Dp4 * 16,
                                  part_bytes + 256 + irc_tc::list_area_bytes(pl->dev.n_out));
