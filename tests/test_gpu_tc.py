@@ -162,3 +162,23 @@ def test_unreferenced_rows_do_not_matter(gpu, mode):
     r2 = irc.site_knn(irc.Plan(plan2), torch.from_numpy(F2).to(gpu), 30, mode)
     assert np.array_equal(r1["miKnn"].cpu().numpy(), r2["miKnn"].cpu().numpy())
     assert np.array_equal(r1["rho"].cpu().numpy().view(np.int32), r2["rho"].cpu().numpy().view(np.int32))
+
+
+@pytest.mark.parametrize("mode", ["bf16", "fp8"])
+def test_list_area_overflow_goes_to_the_exact_fallback(gpu, mode):
+    """Every candidate at one distance: each query lists all 200 candidates,
+    more than the list area's 128 per query on average, so later warps'
+    allocations fail and their queries are finished by the exact fallback;
+    the results still equal the EXACT form (ties by index) bit for bit."""
+    rng = np.random.default_rng(5)
+    a = rng.normal(0, 3, 24).astype(np.float32)
+    b = a + np.float32(2.0)
+    F = np.concatenate([np.tile(a, (128, 1)), np.tile(b, (200, 1))]).astype(np.float32)
+    plan = dict(q0=np.array([0], np.int32), nq=np.array([128], np.int32), roff=np.array([0, 1], np.int32),
+                rs=np.array([128], np.int32), rn=np.array([200], np.int32), q_base=0, n_out=128, n_f=F.shape[0])
+    Fd = torch.from_numpy(F).to(gpu)
+    ex = irc.site_knn(irc.Plan(plan), Fd, 30, "exact")
+    tc = irc.site_knn(irc.Plan(plan), Fd, 30, mode)
+    assert np.array_equal(tc["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy())
+    assert np.array_equal(tc["rho"].cpu().numpy().view(np.int32), ex["rho"].cpu().numpy().view(np.int32))
+    assert (tc["miKnn"].cpu().numpy() == np.arange(129, 159)[None, :]).all()
