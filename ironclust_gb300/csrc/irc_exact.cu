@@ -298,11 +298,14 @@ __global__ void k_delta_list(irc::PlanDev p, const float *__restrict__ R, int kn
 }
 
 // One CTA per chunk: compact the chunk's flagged queries (in order) into the
-// chunk's own segment of fb_list, then claim one (chunk, 16-query tile) item
-// per started 16 of them.  item = {chunk, (first << 5) | count}.
+// chunk's own segment of fb_list, then claim the (16-query tile, part) units
+// of the fallback scan: unit = {chunk | part << 28, (first << 5) | count}.
+constexpr int kParts = 8;        // most parts of one candidate window (part < 2^3: 3 bits at bit 28)
+constexpr int kMinPart = 2048;   // fewest candidates of a part
+
 __global__ void __launch_bounds__(kThreads)
 k_delta_compact(irc::PlanDev p, const int *__restrict__ fb_flag, int *__restrict__ fb_list,
-                int *__restrict__ n_items, int2 *__restrict__ items)
+                int *__restrict__ n_items, int2 *__restrict__ items, unsigned long long *__restrict__ keys)
 {
     __shared__ int wsum[kThreads / 32];
     __shared__ int running, base;
@@ -318,25 +321,40 @@ k_delta_compact(irc::PlanDev p, const int *__restrict__ fb_flag, int *__restrict
         __syncthreads();
         int off = running;
         for (int w = 0; w < warp; ++w) off += wsum[w];
-        if (f) fb_list[seg + off + __popc(bal & ((1u << lane) - 1u))] = q0 + i;
+        if (f) {
+            fb_list[seg + off + __popc(bal & ((1u << lane) - 1u))] = q0 + i;
+            keys[seg + i] = ~0ull;
+        }
         __syncthreads();
         if (threadIdx.x == 0) for (int w = 0; w < kThreads / 32; ++w) running += wsum[w];
         __syncthreads();
     }
     const int total = running, ntile = (total + kQB - 1) / kQB;
-    if (threadIdx.x == 0) base = ntile ? atomicAdd(n_items, ntile) : 0;
+    // a long candidate window is split into np parts of at least kMinPart
+    const int np = min(kParts, max(1, __ldg(p.ncand + chunk) / kMinPart)), nunit = ntile * np;
+    if (threadIdx.x == 0) base = nunit ? atomicAdd(n_items, nunit) : 0;
     __syncthreads();
-    for (int j = threadIdx.x; j < ntile; j += kThreads)
-        items[base + j] = make_int2(chunk, ((j * kQB) << 5) | min(kQB, total - j * kQB));
+    for (int j = threadIdx.x; j < nunit; j += kThreads) {
+        const int t = j / np, part = j - t * np;
+        items[base + j] = make_int2(chunk | (part << 28), ((t * kQB) << 5) | min(kQB, total - t * kQB));
+    }
 }
 
-// Drift-window fallback, 16 queued queries of one chunk per CTA: every
-// linked candidate is loaded once for the 16 and kept per query when its rho
-// exceeds the query's (the search_delta_drift mask), ties by (d2, index).
+// Drift-window fallback for the queued queries, one unit per (16-query tile
+// of a chunk, part of its candidate window; long windows have up to kParts
+// parts of at least kMinPart candidates): a unit loads every candidate of its
+// part once for the 16 queries, keeps per
+// query the candidates whose rho exceeds the query's (the search_delta_drift
+// mask), ties by (d2, index), and folds its best key into the query's key
+// with a 64-bit atomicMin -- the minimum of the same keys in any order, so
+// the split changes no result while giving the SMs kParts times more units
+// (a probe holds ~1,000 fallback tiles per site, too few to fill 152 SMs
+// when each scans a whole ~30K-candidate window).
+
 __global__ void __launch_bounds__(kThreads)
 k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restrict__ R, int nC,
               const int *__restrict__ n_items, const int2 *__restrict__ items, const int *__restrict__ fb_list,
-              float *__restrict__ delta, int *__restrict__ nneigh)
+              unsigned long long *__restrict__ keys)
 {
     __shared__ __align__(16) float sA[IRC_NC_MAX * kQB];
     __shared__ float sRA[kQB];
@@ -344,9 +362,12 @@ k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restri
     __shared__ unsigned long long red[kQB][kThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int total = *n_items;
-    for (int it = blockIdx.x; it < total; it += gridDim.x) {
-        const int2 item = items[it];
-        const int chunk = item.x, first = item.y >> 5, n = item.y & 31;
+    for (int u = blockIdx.x; u < total; u += gridDim.x) {
+        const int2 item = items[u];
+        const int chunk = item.x & 0x0fffffff, part = item.x >> 28, first = item.y >> 5, n = item.y & 31;
+        const int ntot = __ldg(p.ncand + chunk);
+        const int np = min(kParts, max(1, ntot / kMinPart));
+        const int r0 = __ldg(p.roff + chunk), r1 = __ldg(p.roff + chunk + 1);
         const int seg = __ldg(p.q0 + chunk) - p.q_base;
         if (threadIdx.x < kQB) {
             const int q = fb_list[seg + first + min((int)threadIdx.x, n - 1)];
@@ -362,10 +383,12 @@ k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restri
         unsigned long long best[kQB];
 #pragma unroll
         for (int q = 0; q < kQB; ++q) best[q] = ~0ull;
-        const int r0 = __ldg(p.roff + chunk), r1 = __ldg(p.roff + chunk + 1);
-        for (int r = r0; r < r1; ++r) {
+        const int per = (ntot + np - 1) / np, lo = part * per, hi = min(ntot, lo + per);
+        int pos = 0;                                         // position of run r's first candidate
+        for (int r = r0; r < r1 && pos < hi; ++r) {
             const int rs = __ldg(p.rs + r), rn = __ldg(p.rn + r);
-            for (int i = threadIdx.x; i < rn; i += kThreads) {
+            const int a = max(lo - pos, 0), b = min(hi - pos, rn);
+            for (int i = a + (int)threadIdx.x; i < b; i += kThreads) {
                 const int iB = rs + i;
                 const float rb = __ldg(R + iB);
                 unsigned live = 0;
@@ -382,6 +405,7 @@ k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restri
                         best[q] = key < best[q] ? key : best[q];
                     }
             }
+            pos += rn;
         }
 #pragma unroll
         for (int q = 0; q < kQB; ++q) {
@@ -390,17 +414,34 @@ k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restri
         }
         __syncthreads();
         if (threadIdx.x < n) {
-            const int q = threadIdx.x;
-            unsigned long long b = red[q][0];
-            for (int w = 1; w < kThreads / 32; ++w) b = red[q][w] < b ? red[q][w] : b;
-            const int qq = sQ[q];
-            const size_t o = (size_t)(qq - p.q_base);
-            const bool ok = b != ~0ull;
-            const float d2 = ok ? __uint_as_float((unsigned)(b >> 32)) : kInfSentinel;
-            delta[o] = __fmul_rn(irc::ref_sqrt_abs(d2), sRA[q]);
-            nneigh[o] = (ok ? (int)(b & 0xffffffffu) : qq) + 1;
+            unsigned long long b = red[threadIdx.x][0];
+            for (int w = 1; w < kThreads / 32; ++w) b = red[threadIdx.x][w] < b ? red[threadIdx.x][w] : b;
+            if (b != ~0ull) atomicMin(keys + (sQ[threadIdx.x] - p.q_base), b);
         }
         __syncthreads();
+    }
+}
+
+// delta and nneigh of the queued queries from their keys (no candidate:
+// sqrt(SINGLE_INF) .* rho and the query itself, as search_delta_drift_).
+__global__ void k_delta_finish(irc::PlanDev p, const float *__restrict__ R, const int *__restrict__ n_items,
+                               const int2 *__restrict__ items, const int *__restrict__ fb_list,
+                               const unsigned long long *__restrict__ keys, float *__restrict__ delta,
+                               int *__restrict__ nneigh)
+{
+    const int total = *n_items * kQB;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int2 item = items[t / kQB];
+        const int j = t - (t / kQB) * kQB;
+        const int chunk = item.x & 0x0fffffff, first = item.y >> 5, n = item.y & 31;
+        if ((item.x >> 28) != 0 || j >= n) continue;        // each tile once (its part 0)
+        const int qq = fb_list[__ldg(p.q0 + chunk) - p.q_base + first + j];
+        const size_t o = (size_t)(qq - p.q_base);
+        const unsigned long long b = keys[o];
+        const bool ok = b != ~0ull;
+        const float d2 = ok ? __uint_as_float((unsigned)(b >> 32)) : kInfSentinel;
+        delta[o] = __fmul_rn(irc::ref_sqrt_abs(d2), __ldg(R + qq));
+        nneigh[o] = (ok ? (int)(b & 0xffffffffu) : qq) + 1;
     }
 }
 
@@ -447,15 +488,19 @@ int irc_site_delta_list(irc_plan *pl, const float *F, int nC, const float *R, in
     // flags in list a, compacted queries in list b, (chunk, tile) items after them
     int *n_items = cnt + irc::kScratchItems;
     int2 *items = reinterpret_cast<int2 *>(lb + pl->dev.n_out);
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(
+        lb + pl->dev.n_out + 16 * ((size_t)pl->dev.n_out / 16 + pl->dev.nChunks + 1));
     cudaError_t e = cudaMemsetAsync(n_items, 0, sizeof(int), s);
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_delta: memset");
     const int n = pl->dev.n_out;
     k_delta_list<<<(n + 255) / 256, 256, 0, s>>>(pl->dev, R, knn, miKnn, d2Knn, delta, nneigh, la);
     IRC_CHECK_LAUNCH("irc_site_delta list");
-    k_delta_compact<<<pl->dev.nChunks, kThreads, 0, s>>>(pl->dev, la, lb, n_items, items);
+    k_delta_compact<<<pl->dev.nChunks, kThreads, 0, s>>>(pl->dev, la, lb, n_items, items, keys);
     IRC_CHECK_LAUNCH("irc_site_delta compact");
-    k_delta_tiles<<<kQueueBlocks, kThreads, 0, s>>>(pl->dev, F, R, nC, n_items, items, lb, delta, nneigh);
+    k_delta_tiles<<<kQueueBlocks, kThreads, 0, s>>>(pl->dev, F, R, nC, n_items, items, lb, keys);
     IRC_CHECK_LAUNCH("irc_site_delta tiles");
+    k_delta_finish<<<kQueueBlocks, kThreads, 0, s>>>(pl->dev, R, n_items, items, lb, keys, delta, nneigh);
+    IRC_CHECK_LAUNCH("irc_site_delta finish");
     return IRC_OK;
 }
 
@@ -593,6 +638,7 @@ extern "C" int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t 
     p.q0 = d_q0; p.nq = d_nq; p.roff = d_roff; p.rs = d_rs; p.rn = d_rn;
     p.roffr = d_roff; p.rsr = d_rs; p.rnr = d_rn;         // the EXACT kernels take any run split
     for (int k = 0; k < irc::kNumTileSizes; ++k) p.tile_off[k] = d_tile;     // only the 16-query table is read
+    p.ncand = nullptr;                                    // read only by the delta kernels
     p.nChunks = nChunks; p.q_base = q_base; p.n_out = n_out; p.nF = nF; p.nRuns = nRuns;
     const size_t smem = (size_t)kQB * kCap * 8 + (size_t)kQB * kThreads * 4;
     e = cudaFuncSetAttribute(k_site_knn_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

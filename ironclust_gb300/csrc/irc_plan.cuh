@@ -40,6 +40,7 @@ struct PlanDev {
     const int32_t *q0, *nq, *roff, *rs, *rn;
     const int32_t *roffr, *rsr, *rnr;
     const int32_t *tile_off[kNumTileSizes];   // [nChunks+1] prefix sums of ceil(nq/QB)
+    const int32_t *ncand;                     // [nChunks] candidates of each chunk (sum of its runs)
     int nChunks, q_base, n_out, nF, nRuns;
 };
 

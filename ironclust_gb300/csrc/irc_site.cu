@@ -373,6 +373,10 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
         irc_host::set_error("irc_plan_create: null pointer or empty plan");
         return IRC_E_INVAL;
     }
+    if (nChunks >= (1 << 28)) {                       // chunk ids share a word with a 3-bit part number
+        irc_host::set_error("irc_plan_create: %d chunks (at most 2^28 - 1)", nChunks);
+        return IRC_E_INVAL;
+    }
     *out = nullptr;
     const int nRuns = roff[nChunks];
     if (roff[0] != 0 || nRuns <= 0) { irc_host::set_error("irc_plan_create: bad roff"); return IRC_E_INVAL; }
@@ -423,6 +427,12 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     size_t off_roffr = img.size(); img.insert(img.end(), roff, roff + nCh + 1);
     size_t off_rsr = img.size(); img.insert(img.end(), rs, rs + nRuns);
     size_t off_rnr = img.size(); img.insert(img.end(), rn, rn + nRuns);
+    size_t off_ncand = img.size();
+    for (int i = 0; i < nChunks; ++i) {
+        int32_t c = 0;
+        for (int r = roff[i]; r < roff[i + 1]; ++r) c += rn[r];
+        img.push_back(c);
+    }
     size_t off_tile[irc::kNumTileSizes];
     for (int k = 0; k < irc::kNumTileSizes; ++k) {
         const int qb = irc::kTileSizes[k];
@@ -446,7 +456,11 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     if (img.size() & 1) img.push_back(0);          // scratch starts 8-byte aligned (int2 items)
     // 4 words, two query lists of n_out, and the (chunk, tile) items of the
     // delta fallback: at most n_out/16 + nChunks pairs
-    const size_t scratch_ints = irc::kScratchLists + 2 * (size_t)n_out + 2 * ((size_t)n_out / 16 + nChunks + 1);
+    // counters, two query lists, the delta fallback's (tile, part) units (up to 8 parts per
+    // 16-query tile) and its per-query 64-bit best keys (8-byte aligned: every term before
+    // them is even)
+    const size_t scratch_ints = irc::kScratchLists + 2 * (size_t)n_out +
+                                16 * ((size_t)n_out / 16 + nChunks + 1) + 2 * (size_t)n_out;
     cudaError_t e = cudaMalloc(&pl->dmem, (img.size() + scratch_ints) * sizeof(int32_t));
     if (e != cudaSuccess) {
         free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn); free(pl);
@@ -464,6 +478,7 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     pl->dev.roffr = base + off_roffr;
     pl->dev.rsr = base + off_rsr;
     pl->dev.rnr = base + off_rnr;
+    pl->dev.ncand = base + off_ncand;
     for (int k = 0; k < irc::kNumTileSizes; ++k) pl->dev.tile_off[k] = base + off_tile[k];
     pl->scratch = (int32_t *)pl->dmem + img.size();
     pl->tc_items = reinterpret_cast<const irc::TcItem *>((const int32_t *)pl->dmem + off_items);
