@@ -263,7 +263,7 @@ def run_ours(args):
                 roof = {"bound": "fp32-simt", "kernel": dom_name, "achieved": ach, "peak": fp32_peak,
                         "unit": "TFLOP/s", "frac": ach / fp32_peak, "traffic": None,
                         "peak_src": "nominal 152 SM x 128 lanes x 2.07 GHz"}
-        n_launch = {"ref": 2, "exact": 5, "bf16": 9, "fp8": 10}
+        n_launch = {"ref": 2, "exact": 6, "bf16": 10, "fp8": 11}
         out = {
             "metric": METRIC, "value": hr.get("spikes_per_s"), "unit": "spikes/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": hr.get("ms_per_step"),
