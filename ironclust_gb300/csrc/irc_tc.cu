@@ -143,10 +143,10 @@ __device__ __forceinline__ void ld_nc_v8(const float *p, float (&v)[8])
 // warp-cooperative; o = q - q_base.  Requires knn <= 32.  Candidate e is
 // lane e % 32 of round e / 32, and every lane gathers its own rows.
 template <int PER>
-__device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL, int q,
+__device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL, bool complete, int q,
                                        const float *__restrict__ F, const float4 *__restrict__ Fp, int Dp4,
                                        float4 *__restrict__ qs, int nC, int knn, size_t o, unsigned long long *ws,
-                                       int lane, int *miKnn, float *d2Knn, float *vrKnn, float *rho)
+                                       int lane, int *miKnn, float *d2Knn, float *vrKnn, float *rho, int *scratch)
 {
     const float *a = F + (size_t)q * nC;
     // the query row, staged once per warp (broadcast reads below)
@@ -181,6 +181,22 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
             }
             if (acc > 0.0f && acc < IRC_SINGLE_INF_F)
                 kv[bi] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
+        }
+    }
+    // A list cut by tau that holds fewer than knn + 16 positive distances
+    // (exact copies of the query, at distance 0 and excluded like the
+    // reference's d > 0 test, crowded the threshold) may miss nearer
+    // distinct candidates: such a query goes to the exact fallback.
+    if (!complete) {
+        unsigned nv = 0;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) nv += kv[i] != ~0ull;
+        if (__reduce_add_sync(0xffffffffu, nv) < (unsigned)(knn + 16)) {
+            if (lane == 0) {
+                const int k = atomicAdd(scratch + 0, 1);
+                scratch[irc::kScratchLists + k] = q;
+            }
+            return;
         }
     }
     // ws[0 .. WARP_KEYS) <- the WARP_KEYS smallest keys, ascending.  With
@@ -492,7 +508,9 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
             const int k = atomicAdd(scratch + 0, 1);
             scratch[irc::kScratchLists + k] = q;
         } else {
-            lo.qinfo[q - p.q_base] = make_int2((int)(base + incl - len), cL);
+            // bit 30: the list holds every candidate of the chunk (nothing was cut by tau)
+            const int complete = cL == __ldg(p.ncand + it.chunk[s]) ? (1 << 30) : 0;
+            lo.qinfo[q - p.q_base] = make_int2((int)(base + incl - len), cL | complete);
         }
     }
     if (!fits) return;
@@ -700,7 +718,7 @@ constexpr int RR_WARPS = 8;
 __global__ void __launch_bounds__(32 * RR_WARPS, 4)
 k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int n_out, int q_base,
          const float *__restrict__ F, const float4 *__restrict__ Fp, int nC, int knn, float *__restrict__ vrKnn,
-         float *__restrict__ rho, int *__restrict__ miKnn, float *__restrict__ d2Knn)
+         float *__restrict__ rho, int *__restrict__ miKnn, float *__restrict__ d2Knn, int *__restrict__ scratch)
 {
     __shared__ unsigned long long wkeys[RR_WARPS * WARP_KEYS];
     __shared__ float4 qrows[RR_WARPS * QROW4];
@@ -711,15 +729,19 @@ k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int
     if (qi.x < 0) return;
     const int Dp4 = irc_tc::fp_row4(nC);
     const uint32_t *lst = lists + (unsigned)qi.x;
-    const int cL = qi.y, q = q_base + o;
+    const int cL = qi.y & 0x3fffffff, q = q_base + o;
+    const bool complete = (qi.y >> 30) & 1;
     unsigned long long *ws = wkeys + warp * WARP_KEYS;
     float4 *qs = qrows + warp * QROW4;
     if (cL <= 64)
-        rerank<2>(lst, cL, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        rerank<2>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho,
+                  scratch);
     else if (cL <= 128)
-        rerank<4>(lst, cL, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        rerank<4>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho,
+                  scratch);
     else
-        rerank<8>(lst, cL, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho);
+        rerank<8>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho,
+                  scratch);
 }
 
 }  // namespace
@@ -760,8 +782,8 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
     kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, nk, lo, pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
     if (ev) cudaEventRecord(ev[1], s);
-    k_rerank<<<(n_out + RR_WARPS - 1) / RR_WARPS, 32 * RR_WARPS, 0, s>>>(lo.qinfo, lo.lists, n_out, pl->dev.q_base, F,
-                                                                         Fp, nC, knn, vrKnn, rho, miKnn, d2Knn);
+    k_rerank<<<(n_out + RR_WARPS - 1) / RR_WARPS, 32 * RR_WARPS, 0, s>>>(
+        lo.qinfo, lo.lists, n_out, pl->dev.q_base, F, Fp, nC, knn, vrKnn, rho, miKnn, d2Knn, pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core) re-rank");
     if (ev) cudaEventRecord(ev[2], s);
     return IRC_OK;

@@ -182,3 +182,23 @@ def test_list_area_overflow_goes_to_the_exact_fallback(gpu, mode):
     assert np.array_equal(tc["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy())
     assert np.array_equal(tc["rho"].cpu().numpy().view(np.int32), ex["rho"].cpu().numpy().view(np.int32))
     assert (tc["miKnn"].cpu().numpy() == np.arange(129, 159)[None, :]).all()
+
+
+@pytest.mark.parametrize("mode", ["bf16", "fp8"])
+def test_mass_exact_duplicates_keep_the_nearest_distinct_neighbours(gpu, mode):
+    """A query with 100 exact copies among its candidates: every copy is at
+    distance 0, which the path excludes (as search_min_drift's d > 0 test
+    does), so the kNN are the nearest distinct spikes.  The filter's
+    threshold collapses onto the copies; the re-rank must not return fewer
+    neighbours than the EXACT form."""
+    rng = np.random.default_rng(9)
+    a = rng.normal(0, 3, 24).astype(np.float32)
+    others = (a + rng.normal(0, 1.0, (200, 24))).astype(np.float32)
+    F = np.concatenate([np.tile(a, (100, 1)), others]).astype(np.float32)
+    plan = dict(q0=np.array([0], np.int32), nq=np.array([100], np.int32), roff=np.array([0, 1], np.int32),
+                rs=np.array([0], np.int32), rn=np.array([300], np.int32), q_base=0, n_out=100, n_f=F.shape[0])
+    Fd = torch.from_numpy(F).to(gpu)
+    ex = irc.site_knn(irc.Plan(plan), Fd, 30, "exact")
+    tc = irc.site_knn(irc.Plan(plan), Fd, 30, mode)
+    assert np.array_equal(tc["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy())
+    assert np.array_equal(tc["rho"].cpu().numpy().view(np.int32), ex["rho"].cpu().numpy().view(np.int32))
