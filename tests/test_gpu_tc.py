@@ -202,3 +202,41 @@ def test_mass_exact_duplicates_keep_the_nearest_distinct_neighbours(gpu, mode):
     tc = irc.site_knn(irc.Plan(plan), Fd, 30, mode)
     assert np.array_equal(tc["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy())
     assert np.array_equal(tc["rho"].cpu().numpy().view(np.int32), ex["rho"].cpu().numpy().view(np.int32))
+
+
+@pytest.mark.parametrize("knn,d", [(1, 24), (7, 3), (32, 58), (16, 52)])
+@pytest.mark.parametrize("mode", ["bf16", "fp8"])
+def test_knn_and_dimension_edges(gpu, knn, d, mode):
+    """k from 1 to the 32 the tensor-core forms serve, feature counts from 3 to
+    the largest a 128-byte operand row holds (58 BF16 / 52 FP8 features):
+    rows the filter kept whole equal the EXACT form bit for bit, and recall
+    stays at the form's bar (BF16 0.999; FP8 is measured, not guaranteed)."""
+    if mode == "fp8" and d > 52:
+        pytest.skip("FP8 rows hold at most 52 features")
+    F, plan, _ = small_site(n=2500, d=d, n_chunks=4, seed=20 + knn)
+    Fd = torch.from_numpy(F).to(gpu)
+    P = irc.Plan(plan)
+    tc = irc.site_knn(P, Fd, knn=knn, mode=mode)
+    ex = irc.site_knn(P, Fd, knn=knn, mode="exact")
+    mt, me = tc["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy()
+    assert mt.shape == (plan["n_out"], knn)
+    same = np.all(mt == me, axis=1)
+    d2t, d2e = tc["d2Knn"].cpu().numpy(), ex["d2Knn"].cpu().numpy()
+    assert np.array_equal(d2t[same].view(np.int32), d2e[same].view(np.int32))
+    assert recall(mt, me) >= (0.999 if mode == "bf16" else 0.95)
+
+
+@pytest.mark.parametrize("mode", ["bf16", "fp8"])
+def test_fewer_candidates_than_k(gpu, mode):
+    """Chunks linked to fewer candidates than k: every candidate is listed
+    (complete lists), the missing neighbours are the sentinel, as in the
+    EXACT form."""
+    rng = np.random.default_rng(3)
+    F = rng.normal(0, 2, (40, 24)).astype(np.float32)
+    plan = dict(q0=np.array([0, 20], np.int32), nq=np.array([20, 20], np.int32), roff=np.array([0, 1, 2], np.int32),
+                rs=np.array([0, 20], np.int32), rn=np.array([20, 20], np.int32), q_base=0, n_out=40, n_f=40)
+    Fd = torch.from_numpy(F).to(gpu)
+    tc = irc.site_knn(irc.Plan(plan), Fd, 30, mode)
+    ex = irc.site_knn(irc.Plan(plan), Fd, 30, "exact")
+    assert np.array_equal(tc["miKnn"].cpu().numpy(), ex["miKnn"].cpu().numpy())
+    assert np.array_equal(tc["vrKnn"].cpu().numpy().view(np.int32), ex["vrKnn"].cpu().numpy().view(np.int32))
