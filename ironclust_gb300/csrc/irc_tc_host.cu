@@ -107,7 +107,7 @@ template <bool FP8>
 __global__ void __launch_bounds__(32 * kPrepWarps)
 k_prep(const float *__restrict__ F, int lo, int n, int nC, const float *__restrict__ ref,
        const unsigned *__restrict__ amax, uint4 *__restrict__ Fq, uint4 *__restrict__ Fc, float *__restrict__ Fp,
-       int Dp4)
+       int Dp4, int q_lo, int q_hi)
 {
     extern __shared__ __align__(16) unsigned char prep_sm[];
     const int nCs = nC | 1;
@@ -216,10 +216,11 @@ k_prep(const float *__restrict__ F, int lo, int n, int nC, const float *__restri
         }
     }
     __syncwarp();
+    // query rows (the plan's own queries, q_lo .. q_hi-1) are only read as query operands
     uint4 *gq = Fq + (size_t)r0 * 8, *gc = Fc + (size_t)r0 * 8;
     for (int t = lane; t < nr * 8; t += 32) {
         const int r = t >> 3, j = t & 7;
-        gq[t] = sq[r * 8 + (j ^ (r & 7))];
+        if (r0 + r >= q_lo && r0 + r < q_hi) gq[t] = sq[r * 8 + (j ^ (r & 7))];
         gc[t] = sc[r * 8 + (j ^ (r & 7))];
     }
 }
@@ -316,7 +317,8 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
         const int lo = pl->row_iv[2 * v], n = pl->row_iv[2 * v + 1] - lo;
         const int rows_per_block = 32 * kPrepWarps;
         prep<<<(n + rows_per_block - 1) / rows_per_block, 32 * kPrepWarps, psm, s>>>(
-            F, lo, n, nC, ref, amax, (uint4 *)fq, (uint4 *)fc, (float *)fp, Dp4);
+            F, lo, n, nC, ref, amax, (uint4 *)fq, (uint4 *)fc, (float *)fp, Dp4, pl->dev.q_base,
+            pl->dev.q_base + pl->dev.n_out);
     }
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core) prep");
     CUtensorMap mq, mc;
