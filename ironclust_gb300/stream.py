@@ -59,24 +59,6 @@ def band_members(offs, n_link=15, band=64):
     return out
 
 
-def site_plan_from_members(lim, members, base):
-    """Plan of one site whose spikes are split into chunks by lim [n+1] (0-based
-    limits, chunk ids shared with the recording), every spike a query, candidate
-    runs = the linked chunks' spikes (non-empty ones, ascending chunk id).  Row
-    indices offset by base."""
-    lim = np.asarray(lim, np.int64)
-    cnt = np.diff(lim)
-    ne = cnt > 0
-    q = np.flatnonzero(ne)
-    mem = members[:, q]
-    keep = ne[mem]
-    per = keep.sum(0)
-    b = mem.T[keep.T]
-    i32 = lambda v: np.asarray(v, np.int32)
-    return dict(q0=i32(lim[q] + base), nq=i32(cnt[q]), roff=i32(np.concatenate([[0], np.cumsum(per)])),
-                rs=i32(lim[b] + base), rn=i32(cnt[b]))
-
-
 def make_workload(n_sites=384, total=100_000_000, n_chunks=10_000, n_dim=33, seed=1004, drift_sd=0.3,
                   drift_slope=0.01, noise_frac=0.05, n_link=15, band=64, block_chunks=128, pin=True):
     """Synthetic recording of the multi-day shape in block-major order.
