@@ -302,6 +302,19 @@ def run_ours(args):
     return out
 
 
+def min_time_roofline(flops, nbytes, ms, peaks):
+    """Roofline of a small-tile workload: the minimum time is the larger of
+    its algorithmic flops at the sustained BF16 tensor rate and its
+    compulsory bytes at the HBM rate; frac = that minimum / the measured
+    time.  Both terms are reported."""
+    t_tc = flops / (peaks["bf16_sus"] * 1e12) * 1e3
+    t_hbm = nbytes / (peaks["hbm"] * 1e9) * 1e3
+    return {"flops": flops, "bytes": nbytes, "t_tensor_ms": t_tc, "t_hbm_ms": t_hbm,
+            "bound": "tensor" if t_tc >= t_hbm else "hbm", "min_ms": max(t_tc, t_hbm), "measured_ms": ms,
+            "frac": max(t_tc, t_hbm) / ms, "peaks": "%s: bf16 sustained %.1f TFLOP/s, HBM %.1f GB/s" % (
+                peaks["src"], peaks["bf16_sus"], peaks["hbm"])}
+
+
 def run_batched(args, dev, torch, irc, flush, stream):
     """The probe-scale batch (384 sites, 10M spikes, D in {18, 24, 33}, 1,200
     drift chunks): all sites in one plan, one launch per kernel, the whole
@@ -317,6 +330,16 @@ def run_batched(args, dev, torch, irc, flush, stream):
     res = {"workload": "probe10m" if args.probe_sites == 384 else "probe%d" % args.probe_sites,
            "sites": b.n_sites, "spikes": N, "chunks": int(len(b.plan["q0"])), "pairs": plan_pairs(b.plan),
            "dims": sorted(set(int(d) for d in b.dims)), "generation_s": gen_s, "forms": {}}
+    # algorithmic work: 2*D_site flops per pair (each site at its own D); compulsory bytes: every
+    # site's features read once (4*D_site each) + the outputs (knn indices and d2, rho, delta, nneigh)
+    pl = b.plan
+    roff, rn = np.asarray(pl["roff"], np.int64), np.asarray(pl["rn"], np.int64)
+    csum = np.concatenate([[0], np.cumsum(rn)])
+    ncand = csum[roff[1:]] - csum[roff[:-1]]
+    dsite = np.asarray(b.dims, np.int64)[np.asarray(b.site_of_chunk)]
+    alg_flops = float(np.sum(2 * dsite * np.asarray(pl["nq"], np.int64) * ncand))
+    alg_bytes = float(np.sum(np.asarray(b.sizes) * np.asarray(b.dims) * 4) + N * (KNN * 8 + 12))
+    peaks = _peaks()
     from ironclust_gb300 import autotune
     outs = {}
     for mode in [m.strip() for m in args.batched_forms.split(",") if m.strip()]:
@@ -356,7 +379,8 @@ def run_batched(args, dev, torch, irc, flush, stream):
             graph.append(e0.elapsed_time(e1))
         ms_e, ms_g = sum(eager) / len(eager), sum(graph) / len(graph)
         res["forms"][mode] = {"ms_eager": ms_e, "ms_graph": ms_g, "spikes_per_s_graph": N / (ms_g / 1e3),
-                              "spikes_per_s_eager": N / (ms_e / 1e3)}
+                              "spikes_per_s_eager": N / (ms_e / 1e3),
+                              "roofline": min_time_roofline(alg_flops, alg_bytes, ms_g, peaks)}
         if tuned:
             res["forms"][mode]["autotune"] = tuned
         outs[mode] = out["miKnn"].clone()
@@ -391,6 +415,11 @@ def run_stream(args, dev, torch, irc):
            "h2d_bytes": h2d, "d2h_bytes": d2h,
            "host_link_gbs": (h2d + d2h) / (sum(ms) / len(ms) / 1e3) / 1e9,
            "data": "synthetic: FP16 features in pinned host memory, random-walk + 0.01/step drift"}
+    # roofline of the device work: 2*D flops per pair; compulsory device bytes: the FP16 features in,
+    # widened once, and the outputs
+    D = wl["n_dim"]
+    res["roofline"] = min_time_roofline(2.0 * D * res["pairs"], float(N * D * (2 + 4) + N * (KNN * 4 + 12)),
+                                        res["ms"], _peaks())
     from oracle import oracle as O
     k = wl["n_blocks"] // 2
     a, z = st.block_rows(k)
