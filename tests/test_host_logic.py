@@ -210,3 +210,15 @@ def test_stream_block_plans_address_the_linked_chunks():
             assert [int(p["rn"][r]) for r in runs] == [lims[s, m + 1] - lims[s, m] for m in want]
             seen += int(p["nq"][i])
         assert seen == p["n_out"]
+
+
+def test_min_time_roofline_reports_both_terms():
+    """bench.min_time_roofline: the minimum time is the larger of the tensor
+    and the HBM term, and frac = minimum / measured."""
+    import bench
+    peaks = dict(hbm=1000.0, bf16=2000.0, bf16_sus=1000.0, src="test")
+    r = bench.min_time_roofline(2e12, 5e9, 10.0, peaks)       # 2 ms of tensor work, 5 ms of bytes
+    assert r["bound"] == "hbm" and abs(r["t_tensor_ms"] - 2.0) < 1e-9 and abs(r["t_hbm_ms"] - 5.0) < 1e-9
+    assert abs(r["min_ms"] - 5.0) < 1e-9 and abs(r["frac"] - 0.5) < 1e-9
+    r = bench.min_time_roofline(8e12, 1e9, 16.0, peaks)
+    assert r["bound"] == "tensor" and abs(r["frac"] - 0.5) < 1e-9
