@@ -264,11 +264,13 @@ int irc_batch_stack(float *F, int nCmax, const float *const *F_sites, const int3
  * cudaMalloc/cudaFree or other allocating routine: the device copy of the
  * plan, its tile table and the overflow queue live in one fixed 8 MiB array
  * inside the library, held by every GPU that loads it until the process
- * exits.  The plan must fit that array: 4 + 2*n_out + 3*nChunks + 2 +
+ * exits.  The plan must fit that array: 4 + 2*n_out + 4*nChunks + 2 +
  * 2*nRuns int32 words <= 2^21 (about a million queries); larger plans are
- * rejected with IRC_E_INVAL and a message.  The first call on a device looks
- * up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  Every call
+ * rejected with IRC_E_INVAL and a message, as are plans irc_plan_create
+ * rejects.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current and keeps it; make that
+ * first call before any stream capture, and do not call the entry point on a
+ * device after cudaDeviceReset (the kept address is then stale).  Every call
  * shares the array and overwrites it, so calls that overlap on the GPU (two
  * streams, two host threads) race: serialise them on one stream.  Outputs
  * equal those of irc_site_knn(IRC_MODE_EXACT) bit for bit. */

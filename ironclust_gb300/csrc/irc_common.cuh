@@ -54,6 +54,16 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long k)
 namespace irc_host {
 void set_error(const char *fmt, ...);
 int cuda_status(cudaError_t e, const char *where);
+// Validation of a plan's host arrays (the meaning irc_plan_create gives
+// them), shared by every entry point that takes them: non-null arrays,
+// 1 <= nChunks < 2^28, roff[0] = 0, strictly increasing roff, every chunk's
+// queries inside both [0, nF) and [q_base, q_base + n_out), every run inside
+// [0, nF); bounds are formed in 64-bit arithmetic.  Returns IRC_OK or
+// IRC_E_INVAL (message prefixed by `who`); on success *pairs and *max_nq
+// (either may be null) receive the plan's (query, candidate) pair count and
+// its largest query chunk.
+int check_plan(const char *who, const int32_t *q0, const int32_t *nq, const int32_t *roff, const int32_t *rs,
+               const int32_t *rn, int nChunks, int q_base, int n_out, int nF, long long *pairs, int *max_nq);
 }  // namespace irc_host
 
 #define IRC_CHECK_LAUNCH(where)                                                    \

@@ -532,7 +532,10 @@ static __device__ __align__(256) int32_t g_noalloc_scratch[kNoAllocWords];
 
 // Device address of g_noalloc_scratch per device, looked up once per device
 // with that device current (a host-side reference to the array is only a
-// stand-in, not a device address).
+// stand-in, not a device address).  The address belongs to the device's
+// primary context: cudaDeviceReset destroys that context and the array with
+// it, so a process that resets a device must not call the entry point on that
+// device afterwards (the cached address would be stale).
 constexpr int kMaxDevices = 64;
 int32_t *g_noalloc_ptr[kMaxDevices];
 std::mutex g_noalloc_mu;
@@ -555,6 +558,28 @@ int noalloc_scratch(int32_t **out)
     }
     *out = g_noalloc_ptr[dev];
     return IRC_OK;
+}
+
+// Word offsets of everything the entry point keeps in the fixed array, in
+// order: the plan scratch words (queue counters), two query queues of n_out,
+// q0 [nChunks], nq [nChunks], roff [nChunks+1], rs [nRuns], rn [nRuns] and
+// the 16-query tile table [nChunks+1].  The size check and the pointers both
+// come from here, so they cannot disagree.
+struct NoAllocLayout {
+    size_t q0, nq, roff, rs, rn, tile, total;
+};
+
+NoAllocLayout noalloc_layout(long long n_out, long long nChunks, long long nRuns)
+{
+    NoAllocLayout L;
+    L.q0 = (size_t)irc::kScratchLists + 2 * (size_t)n_out;
+    L.nq = L.q0 + (size_t)nChunks;
+    L.roff = L.nq + (size_t)nChunks;
+    L.rs = L.roff + (size_t)nChunks + 1;
+    L.rn = L.rs + (size_t)nRuns;
+    L.tile = L.rn + (size_t)nRuns;
+    L.total = L.tile + (size_t)nChunks + 1;
+    return L;
 }
 
 // tile_off[i] = sum_{j<i} ceil(nq[j] / QB), one block, chunked scan.
@@ -587,44 +612,30 @@ extern "C" int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t 
                                           int32_t *miKnn, float *d2Knn, void *stream)
 {
     const char *me = "irc_site_knn_exact_noalloc";
-    if (!F || !q0 || !nq || !roff || !rs || !rn || !vrKnn || !miKnn || nChunks <= 0 || n_out <= 0 || nF <= 0) {
-        irc_host::set_error("%s: null pointer or empty plan", me);
+    if (!F || !vrKnn || !miKnn) {
+        irc_host::set_error("%s: null pointer", me);
         return IRC_E_INVAL;
     }
     if (nC > IRC_NC_MAX) { irc_host::set_error("%s: nC=%d > %d", me, nC, IRC_NC_MAX); return IRC_E_NC; }
     if (nC <= 0 || knn <= 0 || knn > kCap / 2) { irc_host::set_error("%s: bad nC=%d / knn=%d", me, nC, knn); return IRC_E_INVAL; }
+    // the same checks as irc_plan_create (64-bit bounds)
+    int rc = irc_host::check_plan(me, q0, nq, roff, rs, rn, nChunks, q_base, n_out, nF, nullptr, nullptr);
+    if (rc != IRC_OK) return rc;
     const int nRuns = roff[nChunks];
-    const size_t need = (size_t)irc::kScratchLists + 2 * (size_t)n_out + 3 * (size_t)nChunks + 2 + 2 * (size_t)(nRuns > 0 ? nRuns : 0);
-    if (roff[0] != 0 || nRuns <= 0 || need > kNoAllocWords) {
-        irc_host::set_error("%s: plan needs %zu scratch words, the fixed array holds %zu "
-                            "(n_out + 1.5*chunks + runs must stay below ~1M)", me, need, kNoAllocWords);
+    const NoAllocLayout L = noalloc_layout(n_out, nChunks, nRuns);
+    if (L.total > kNoAllocWords) {
+        irc_host::set_error("%s: plan needs %zu scratch words (4 + 2*n_out + 4*chunks + 2 + 2*runs), "
+                            "the fixed array holds %zu", me, L.total, kNoAllocWords);
         return IRC_E_INVAL;
     }
-    int tiles = 0;
-    for (int i = 0; i < nChunks; ++i) {
-        if (nq[i] <= 0 || q0[i] < q_base || q0[i] + nq[i] > q_base + n_out || q0[i] + nq[i] > nF ||
-            roff[i + 1] <= roff[i]) {
-            irc_host::set_error("%s: chunk %d out of range", me, i);
-            return IRC_E_INVAL;
-        }
-        for (int r = roff[i]; r < roff[i + 1]; ++r)
-            if (rs[r] < 0 || rn[r] <= 0 || (long long)rs[r] + rn[r] > nF) {
-                irc_host::set_error("%s: run %d out of range", me, r);
-                return IRC_E_INVAL;
-            }
-        tiles += (nq[i] + kQB - 1) / kQB;
-    }
+    long long tiles = 0;
+    for (int i = 0; i < nChunks; ++i) tiles += (nq[i] + kQB - 1) / kQB;
     int32_t *base = nullptr;
-    int rc = noalloc_scratch(&base);
+    rc = noalloc_scratch(&base);
     if (rc != IRC_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    // layout: scratch words | 2 queues of n_out | q0 | nq | roff | rs | rn | tile table
-    int32_t *d_q0 = base + irc::kScratchLists + 2 * (size_t)n_out;
-    int32_t *d_nq = d_q0 + nChunks;
-    int32_t *d_roff = d_nq + nChunks;
-    int32_t *d_rs = d_roff + nChunks + 1;
-    int32_t *d_rn = d_rs + nRuns;
-    int32_t *d_tile = d_rn + nRuns;
+    int32_t *d_q0 = base + L.q0, *d_nq = base + L.nq, *d_roff = base + L.roff;
+    int32_t *d_rs = base + L.rs, *d_rn = base + L.rn, *d_tile = base + L.tile;
     cudaError_t e = cudaMemsetAsync(base, 0, irc::kScratchLists * sizeof(int32_t), s);    // counters start at zero
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_q0, q0, 4 * (size_t)nChunks, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_nq, nq, 4 * (size_t)nChunks, cudaMemcpyHostToDevice, s);
@@ -644,7 +655,7 @@ extern "C" int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t 
     e = cudaFuncSetAttribute(k_site_knn_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn_exact_noalloc: smem attribute");
     int32_t *cnt = base, *queue = base + irc::kScratchLists;
-    k_site_knn_exact<<<tiles, kThreads, smem, s>>>(p, F, nC, knn, vrKnn, rho, miKnn, d2Knn, cnt, queue);
+    k_site_knn_exact<<<(unsigned)tiles, kThreads, smem, s>>>(p, F, nC, knn, vrKnn, rho, miKnn, d2Knn, cnt, queue);
     IRC_CHECK_LAUNCH("irc_site_knn_exact_noalloc");
     k_exact_overflow<<<kQueueBlocks, 256, 0, s>>>(p, F, nC, knn, cnt, queue, vrKnn, rho, miKnn, d2Knn);
     IRC_CHECK_LAUNCH("irc_site_knn_exact_noalloc overflow");

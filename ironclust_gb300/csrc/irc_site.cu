@@ -369,36 +369,17 @@ extern "C" {
 int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const int32_t *roff,
                     const int32_t *rs, const int32_t *rn, int nChunks, int q_base, int n_out, int nF)
 {
-    if (!out || !q0 || !nq || !roff || !rs || !rn || nChunks <= 0 || n_out <= 0 || nF <= 0) {
+    if (!out) {
         irc_host::set_error("irc_plan_create: null pointer or empty plan");
         return IRC_E_INVAL;
     }
-    if (nChunks >= (1 << 28)) {                       // chunk ids share a word with a 3-bit part number
-        irc_host::set_error("irc_plan_create: %d chunks (at most 2^28 - 1)", nChunks);
-        return IRC_E_INVAL;
-    }
     *out = nullptr;
-    const int nRuns = roff[nChunks];
-    if (roff[0] != 0 || nRuns <= 0) { irc_host::set_error("irc_plan_create: bad roff"); return IRC_E_INVAL; }
     long long pairs = 0;
     int max_nq = 0;
-    for (int i = 0; i < nChunks; ++i) {
-        if (nq[i] <= 0 || q0[i] < 0 || q0[i] + nq[i] > nF || q0[i] < q_base || q0[i] + nq[i] > q_base + n_out ||
-            roff[i + 1] <= roff[i]) {
-            irc_host::set_error("irc_plan_create: chunk %d out of range", i);
-            return IRC_E_INVAL;
-        }
-        long long cand = 0;
-        for (int r = roff[i]; r < roff[i + 1]; ++r) {
-            if (rs[r] < 0 || rn[r] <= 0 || (long long)rs[r] + rn[r] > nF) {
-                irc_host::set_error("irc_plan_create: run %d out of range", r);
-                return IRC_E_INVAL;
-            }
-            cand += rn[r];
-        }
-        pairs += cand * nq[i];
-        max_nq = nq[i] > max_nq ? nq[i] : max_nq;
-    }
+    const int vrc = irc_host::check_plan("irc_plan_create", q0, nq, roff, rs, rn, nChunks, q_base, n_out, nF,
+                                         &pairs, &max_nq);
+    if (vrc != IRC_OK) return vrc;
+    const int nRuns = roff[nChunks];
     irc_plan *pl = (irc_plan *)calloc(1, sizeof(irc_plan));
     if (!pl) return IRC_E_NOMEM;
     // host copies

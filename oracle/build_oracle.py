@@ -23,7 +23,8 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_MATLAB = "/root/reference/matlab"
+# the reference's kernel sources (read-only); absent on machines that only run the prebuilt files
+REFERENCE_MATLAB = os.environ.get("IRC_REFERENCE_MATLAB", "/root/reference/matlab")
 REF_KERNELS = ["search_min_drift", "search_delta_drift", "cuda_knn_index",
                "cuda_delta_knn", "irc_cuda_rho_drift", "irc_cuda_delta_drift", "cuda_knn",
                "cuda_knn_full", "cuda_knn_ib", "irc_cuda_rho", "irc_cuda_delta"]
@@ -48,7 +49,7 @@ def build_oracle_lib(force=False):
     srcs = [os.path.join(HERE, "irc_oracle.c"), os.path.join(HERE, "irc_oracle_cluster.c")]
     out = os.path.join(BUILD, "libirc_oracle.so")
     if force or _stale(out, srcs):
-        _run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+        _run(["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
              + srcs + ["-o", out, "-lm"])
     return out
 
