@@ -214,6 +214,12 @@ def run_ours(args):
             got = irc.site_knn(P, F, KNN, mode)["miKnn"]
             recall[mode] = knn_recall(ref, got, torch)
 
+    # accuracy of every form against the FP64 oracle on every spike of the
+    # workload (outside the timed region; the oracle is the checker)
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        accuracy = accuracy_vs_fp64(P, F, site, plan, forms, results, torch, irc)
+
     # end-to-end through host buffers (headline form)
     e2e = None
     if not results.get(head, {}).get("error"):
@@ -279,11 +285,16 @@ def run_ours(args):
             "launch_ms": launch_ms,
             "autotune": tuned,
             "recall_vs_exact": recall,
+            "accuracy_vs_fp64": accuracy,
             "clocks": hr.get("clocks"),
             "e2e": e2e,
             "roofline": roof,
             "gpu_launches": n_launch.get(head, 0) * args.steps,
         }
+        if accuracy and head in accuracy:
+            out["recall_vs_fp64"] = accuracy[head]["recall_vs_fp64"]
+            out["rho_max_rel_err"] = accuracy[head]["rho_max_rel_err"]
+            out["delta_max_rel_err"] = accuracy[head]["delta_max_rel_err"]
         if batched is not None:
             out["batched"] = batched
         if streamed is not None:
@@ -300,6 +311,23 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return out
+
+
+def accuracy_vs_fp64(P, F, site, plan, forms, results, torch, irc):
+    """kNN recall, rho and delta error of every form against the FP64 oracle
+    on every spike (oracle.accuracy: delta from the FP64 rho; a different
+    nearest higher-rho neighbour is an error unless FP32 and FP64 rho order
+    the two candidates differently, counted apart as rho-order flips)."""
+    from oracle import accuracy as A
+    t0 = time.perf_counter()
+    ref = A.fp64_reference(site["F"], plan, KNN)
+    res = {"fp64_seconds": time.perf_counter() - t0}
+    for mode in forms:
+        if results.get(mode, {}).get("error"):
+            continue
+        o = irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
+        res[mode] = A.compare({k: v.cpu().numpy() for k, v in o.items() if v is not None}, ref)
+    return res
 
 
 def min_time_roofline(flops, nbytes, ms, peaks):
@@ -341,7 +369,14 @@ def run_batched(args, dev, torch, irc, flush, stream):
     alg_bytes = float(np.sum(np.asarray(b.sizes) * np.asarray(b.dims) * 4) + N * (KNN * 8 + 12))
     peaks = _peaks()
     from ironclust_gb300 import autotune
-    outs = {}
+    outs, kept = {}, {}
+    # whole sites drawn (seeded) until they hold >= 1 M spikes: the FP64 check's subsample
+    picked, total = [], 0
+    for s in np.random.default_rng(2024).permutation(b.n_sites):
+        picked.append(int(s))
+        total += int(b.sizes[s])
+        if total >= 1_000_000:
+            break
     for mode in [m.strip() for m in args.batched_forms.split(",") if m.strip()]:
         tuned = None
         if mode in ("bf16", "fp8"):
@@ -384,12 +419,46 @@ def run_batched(args, dev, torch, irc, flush, stream):
         if tuned:
             res["forms"][mode]["autotune"] = tuned
         outs[mode] = out["miKnn"].clone()
+        kept[mode] = {k: torch.cat([out[k][b.site_slice(s)] for s in picked]).cpu().numpy()
+                      for k in ("miKnn", "rho", "delta", "nneigh")}
         del g
     if "exact" in outs:
         for mode, mi in outs.items():
             if mode != "exact":
                 res["forms"][mode]["recall_vs_exact"] = knn_recall(outs["exact"], mi, torch)
     P.close()
+    if not args.no_accuracy and kept:
+        t0 = time.perf_counter()
+        res["accuracy_sample"] = {"sites": len(picked), "spikes": total,
+                                  "what": "whole sites drawn with a seeded permutation until >= 1 M spikes"}
+        res["accuracy_vs_fp64"] = batch_accuracy(b, picked, kept, KNN)
+        res["accuracy_sample"]["fp64_seconds"] = time.perf_counter() - t0
+    return res
+
+
+def batch_accuracy(b, picked, kept, knn):
+    """Accuracy of each batched form on the picked sites against the FP64
+    oracle (site by site, aggregated over all checked spikes)."""
+    from oracle import accuracy as A
+    refs = [A.fp64_reference(np.ascontiguousarray(b.F[b.site_slice(s), :int(b.dims[s])]), b.site_plans[s], knn)
+            for s in picked]
+    res = {}
+    for mode, o in kept.items():
+        stats, off = [], 0
+        for s, ref in zip(picked, refs):
+            n, base = int(b.sizes[s]), int(b.bases[s])
+            part = {k: v[off:off + n] for k, v in o.items()}
+            part["miKnn"] = part["miKnn"] - base
+            part["nneigh"] = part["nneigh"] - base
+            stats.append(A.compare(part, ref))
+            off += n
+        n = sum(x["checked"] for x in stats)
+        res[mode] = {"checked": n,
+                     "recall_vs_fp64": sum(x["recall_vs_fp64"] * x["checked"] for x in stats) / n,
+                     "rho_max_rel_err": max(x["rho_max_rel_err"] for x in stats),
+                     "delta_max_rel_err": max(x["delta_max_rel_err"] for x in stats),
+                     "nneigh_errors": sum(x["nneigh_errors"] for x in stats),
+                     "nneigh_rho_order_flips": sum(x["nneigh_rho_order_flips"] for x in stats)}
     return res
 
 
@@ -719,6 +788,8 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-chunks", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the accuracy checks against the FP64 oracle (run outside the timed regions)")
     ap.add_argument("--batched", dest="batched", action="store_true", default=True,
                     help="also time the probe-scale batch (all sites in one plan, CUDA graph)")
     ap.add_argument("--no-batched", dest="batched", action="store_false")

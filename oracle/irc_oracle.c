@@ -410,6 +410,103 @@ static inline double dist2_f64(const float *b, const float *a, int nC)
     return acc;
 }
 
+/* The exact references below visit the queries of a chunk in blocks of
+ * ORC_QB: every candidate row is read once per block and its distances to the
+ * block's queries are formed side by side (each query's own sum still runs in
+ * feature order, exactly as the one-query loops would form it), which lets
+ * the compiler vectorise across the queries.  Work items are (chunk, block)
+ * pairs over the whole plan, scheduled dynamically. */
+#define ORC_QB 8
+
+typedef struct {
+    int *off;                /* [nChunks + 1] prefix of ceil(nq / ORC_QB) */
+    long total;
+} orc_blocks;
+
+static orc_blocks plan_blocks(const int32_t *nq, int nChunks)
+{
+    orc_blocks b;
+    b.off = (int *)malloc(sizeof(int) * ((size_t)nChunks + 1));
+    b.off[0] = 0;
+    for (int i = 0; i < nChunks; ++i) b.off[i + 1] = b.off[i] + (nq[i] + ORC_QB - 1) / ORC_QB;
+    b.total = b.off[nChunks];
+    return b;
+}
+
+/* chunk of flat block w and the first query / query count of that block */
+static inline int block_chunk(const orc_blocks *b, int nChunks, long w)
+{
+    int lo = 0, hi = nChunks;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (b->off[mid] <= w) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+/* queries q0 .. q0+n-1 transposed into aT[c * ORC_QB + j] (unused lanes
+ * repeat the last query) */
+static inline void stage_f32(float *aT, const float *F, int q0, int n, int nC)
+{
+    for (int j = 0; j < ORC_QB; ++j) {
+        const float *a = F + (size_t)(q0 + (j < n ? j : n - 1)) * nC;
+        for (int c = 0; c < nC; ++c) aT[c * ORC_QB + j] = a[c];
+    }
+}
+
+static inline void stage_f64(double *aT, const float *F, int q0, int n, int nC)
+{
+    for (int j = 0; j < ORC_QB; ++j) {
+        const float *a = F + (size_t)(q0 + (j < n ? j : n - 1)) * nC;
+        for (int c = 0; c < nC; ++c) aT[c * ORC_QB + j] = (double)a[c];
+    }
+}
+
+/* dist2_f64 of candidate row b to the ORC_QB staged queries */
+static inline void dist2_f64_qb(double *out, const float *b, const double *aT, int nC)
+{
+    double acc[ORC_QB];
+    for (int j = 0; j < ORC_QB; ++j) acc[j] = 0.0;
+    for (int c = 0; c < nC; ++c) {
+        const double bc = (double)b[c];
+        for (int j = 0; j < ORC_QB; ++j) {
+            const double d = bc - aT[c * ORC_QB + j];
+            acc[j] += d * d;
+        }
+    }
+    for (int j = 0; j < ORC_QB; ++j) out[j] = acc[j];
+}
+
+/* dist2_fma of candidate row b to the ORC_QB staged queries */
+static inline void dist2_fma_qb(float *out, const float *b, const float *aT, int nC)
+{
+    float acc[ORC_QB];
+    for (int j = 0; j < ORC_QB; ++j) acc[j] = 0.0f;
+    for (int c = 0; c < nC; ++c) {
+        const float bc = b[c];
+        for (int j = 0; j < ORC_QB; ++j) {
+            const float d = bc - aT[c * ORC_QB + j];
+            acc[j] = fmaf(d, d, acc[j]);
+        }
+    }
+    for (int j = 0; j < ORC_QB; ++j) out[j] = acc[j];
+}
+
+/* insert (d, c) into the ascending (d, index) list bd/bi of n <= knn entries */
+#define ORC_TOPK_INSERT(bd, bi, n, knn, d, c)                                                     \
+    do {                                                                                          \
+        if ((n) == (knn) && !((d) < (bd)[(n) - 1] || ((d) == (bd)[(n) - 1] && (c) < (bi)[(n) - 1]))) \
+            break;                                                                                \
+        int p_ = ((n) < (knn)) ? (n)++ : (n) - 1;                                                 \
+        while (p_ > 0 && ((d) < (bd)[p_ - 1] || ((d) == (bd)[p_ - 1] && (c) < (bi)[p_ - 1]))) {   \
+            (bd)[p_] = (bd)[p_ - 1];                                                              \
+            (bi)[p_] = (bi)[p_ - 1];                                                              \
+            --p_;                                                                                 \
+        }                                                                                         \
+        (bd)[p_] = (d);                                                                           \
+        (bi)[p_] = (c);                                                                           \
+    } while (0)
+
 /* Top-knn by (d2, index) for every query of every chunk.  exclude_zero=1
  * drops candidates at distance exactly 0 (self and exact duplicates), as the
  * irc2 GPU kernels do; 0 keeps them, as knn_cpu_ does.  Outputs, indexed by
@@ -420,65 +517,89 @@ void orc_exact_knn_f64(int32_t *idx, double *d2out, const float *F, int nC,
                        const int32_t *rs, const int32_t *rn, int nChunks,
                        int q_base, int knn, int exclude_zero)
 {
-    for (int ch = 0; ch < nChunks; ++ch) {
+    orc_blocks B = plan_blocks(nq, nChunks);
 #pragma omp parallel
-        {
-            double *bd = (double *)malloc(sizeof(double) * (size_t)knn);
-            int *bi = (int *)malloc(sizeof(int) * (size_t)knn);
-#pragma omp for schedule(dynamic, 8)
-            for (int qq = 0; qq < nq[ch]; ++qq) {
-                const int q = q0[ch] + qq;
-                const float *a = F + (size_t)q * nC;
-                int n = 0;
-                for (int r = roff[ch]; r < roff[ch + 1]; ++r)
-                    for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
-                        double d = dist2_f64(F + (size_t)c * nC, a, nC);
+    {
+        double *bd = (double *)malloc(sizeof(double) * (size_t)knn * ORC_QB);
+        int *bi = (int *)malloc(sizeof(int) * (size_t)knn * ORC_QB);
+        double *aT = (double *)malloc(sizeof(double) * (size_t)nC * ORC_QB);
+#pragma omp for schedule(dynamic, 4)
+        for (long w = 0; w < B.total; ++w) {
+            const int ch = block_chunk(&B, nChunks, w);
+            const int qa = q0[ch] + (int)(w - B.off[ch]) * ORC_QB;
+            const int nb = (q0[ch] + nq[ch] - qa) < ORC_QB ? (q0[ch] + nq[ch] - qa) : ORC_QB;
+            int n[ORC_QB] = {0};
+            stage_f64(aT, F, qa, nb, nC);
+            for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+                for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
+                    double dd[ORC_QB];
+                    dist2_f64_qb(dd, F + (size_t)c * nC, aT, nC);
+                    for (int j = 0; j < nb; ++j) {
+                        const double d = dd[j];
                         if (exclude_zero && d == 0.0) continue;
-                        if (n == knn && !(d < bd[n - 1] || (d == bd[n - 1] && c < bi[n - 1]))) continue;
-                        int p = (n < knn) ? n++ : n - 1;
-                        while (p > 0 && (d < bd[p - 1] || (d == bd[p - 1] && c < bi[p - 1]))) {
-                            bd[p] = bd[p - 1]; bi[p] = bi[p - 1]; --p;
-                        }
-                        bd[p] = d; bi[p] = c;
+                        ORC_TOPK_INSERT(bd + (size_t)j * knn, bi + (size_t)j * knn, n[j], knn, d, c);
                     }
-                const size_t o = (size_t)(q - q_base) * knn;
+                }
+            for (int j = 0; j < nb; ++j) {
+                const size_t o = (size_t)(qa + j - q_base) * knn;
                 for (int k = 0; k < knn; ++k) {
-                    idx[o + k] = (k < n) ? bi[k] + 1 : 0;
-                    d2out[o + k] = (k < n) ? bd[k] : NAN;
+                    idx[o + k] = (k < n[j]) ? bi[(size_t)j * knn + k] + 1 : 0;
+                    d2out[o + k] = (k < n[j]) ? bd[(size_t)j * knn + k] : NAN;
                 }
             }
-            free(bd); free(bi);
         }
+        free(bd); free(bi); free(aT);
     }
+    free(B.off);
 }
 
-/* Nearest candidate with strictly higher rho (R indexed like F), distance > 0
- * when exclude_zero, ties by (d2, index).  Outputs indexed by q - q_base:
- * nn (1-based, 0 when none) and d2 (INFINITY when none). */
-void orc_exact_delta_f64(int32_t *nn, double *d2out, const float *F, const float *R, int nC,
+/* Nearest candidate with strictly higher rho (R indexed like F, in double so
+ * that an FP64 rho keeps its own order), distance > 0 when exclude_zero, ties
+ * by (d2, index).  Outputs indexed by q - q_base: nn (1-based, 0 when none)
+ * and d2 (INFINITY when none). */
+void orc_exact_delta_f64(int32_t *nn, double *d2out, const float *F, const double *R, int nC,
                          const int32_t *q0, const int32_t *nq, const int32_t *roff,
                          const int32_t *rs, const int32_t *rn, int nChunks,
                          int q_base, int exclude_zero)
 {
-    for (int ch = 0; ch < nChunks; ++ch) {
-#pragma omp parallel for schedule(dynamic, 8)
-        for (int qq = 0; qq < nq[ch]; ++qq) {
-            const int q = q0[ch] + qq;
-            const float *a = F + (size_t)q * nC;
-            const float ra = R[q];
-            double best = INFINITY;
-            int bi = -1;
+    orc_blocks B = plan_blocks(nq, nChunks);
+#pragma omp parallel
+    {
+        double *aT = (double *)malloc(sizeof(double) * (size_t)nC * ORC_QB);
+#pragma omp for schedule(dynamic, 4)
+        for (long w = 0; w < B.total; ++w) {
+            const int ch = block_chunk(&B, nChunks, w);
+            const int qa = q0[ch] + (int)(w - B.off[ch]) * ORC_QB;
+            const int nb = (q0[ch] + nq[ch] - qa) < ORC_QB ? (q0[ch] + nq[ch] - qa) : ORC_QB;
+            double best[ORC_QB], ra[ORC_QB], rmin = INFINITY;
+            int bi[ORC_QB];
+            for (int j = 0; j < nb; ++j) {
+                best[j] = INFINITY;
+                bi[j] = -1;
+                ra[j] = R[qa + j];
+                if (ra[j] < rmin) rmin = ra[j];
+            }
+            stage_f64(aT, F, qa, nb, nC);
             for (int r = roff[ch]; r < roff[ch + 1]; ++r)
                 for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
-                    if (!(R[c] > ra)) continue;
-                    double d = dist2_f64(F + (size_t)c * nC, a, nC);
-                    if (exclude_zero && d == 0.0) continue;
-                    if (d < best || (d == best && c < bi)) { best = d; bi = c; }
+                    if (!(R[c] > rmin)) continue;          /* masked for every query of the block */
+                    double dd[ORC_QB];
+                    dist2_f64_qb(dd, F + (size_t)c * nC, aT, nC);
+                    for (int j = 0; j < nb; ++j) {
+                        if (!(R[c] > ra[j])) continue;
+                        const double d = dd[j];
+                        if (exclude_zero && d == 0.0) continue;
+                        if (d < best[j] || (d == best[j] && c < bi[j])) { best[j] = d; bi[j] = c; }
+                    }
                 }
-            nn[q - q_base] = bi + 1;
-            d2out[q - q_base] = best;
+            for (int j = 0; j < nb; ++j) {
+                nn[qa + j - q_base] = bi[j] + 1;
+                d2out[qa + j - q_base] = best[j];
+            }
         }
+        free(aT);
     }
+    free(B.off);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -628,36 +749,41 @@ void orc_exact_knn_f32(int32_t *idx, float *d2out, const float *F, int nC,
                        const int32_t *q0, const int32_t *nq, const int32_t *roff,
                        const int32_t *rs, const int32_t *rn, int nChunks, int q_base, int knn)
 {
-    for (int ch = 0; ch < nChunks; ++ch) {
+    orc_blocks B = plan_blocks(nq, nChunks);
 #pragma omp parallel
-        {
-            float *bd = (float *)malloc(sizeof(float) * (size_t)knn);
-            int *bi = (int *)malloc(sizeof(int) * (size_t)knn);
-#pragma omp for schedule(dynamic, 8)
-            for (int qq = 0; qq < nq[ch]; ++qq) {
-                const int q = q0[ch] + qq;
-                const float *a = F + (size_t)q * nC;
-                int n = 0;
-                for (int r = roff[ch]; r < roff[ch + 1]; ++r)
-                    for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
-                        float d = dist2_fma(F + (size_t)c * nC, a, nC);
+    {
+        float *bd = (float *)malloc(sizeof(float) * (size_t)knn * ORC_QB);
+        int *bi = (int *)malloc(sizeof(int) * (size_t)knn * ORC_QB);
+        float *aT = (float *)malloc(sizeof(float) * (size_t)nC * ORC_QB);
+#pragma omp for schedule(dynamic, 4)
+        for (long w = 0; w < B.total; ++w) {
+            const int ch = block_chunk(&B, nChunks, w);
+            const int qa = q0[ch] + (int)(w - B.off[ch]) * ORC_QB;
+            const int nb = (q0[ch] + nq[ch] - qa) < ORC_QB ? (q0[ch] + nq[ch] - qa) : ORC_QB;
+            int n[ORC_QB] = {0};
+            stage_f32(aT, F, qa, nb, nC);
+            for (int r = roff[ch]; r < roff[ch + 1]; ++r)
+                for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
+                    float dd[ORC_QB];
+                    dist2_fma_qb(dd, F + (size_t)c * nC, aT, nC);
+                    for (int j = 0; j < nb; ++j) {
+                        const float d = dd[j];
                         if (!(d > 0.0f) || !(d < ORC_SINGLE_INF)) continue;
-                        if (n == knn && !(d < bd[n - 1] || (d == bd[n - 1] && c < bi[n - 1]))) continue;
-                        int p = (n < knn) ? n++ : n - 1;
-                        while (p > 0 && (d < bd[p - 1] || (d == bd[p - 1] && c < bi[p - 1]))) {
-                            bd[p] = bd[p - 1]; bi[p] = bi[p - 1]; --p;
-                        }
-                        bd[p] = d; bi[p] = c;
+                        ORC_TOPK_INSERT(bd + (size_t)j * knn, bi + (size_t)j * knn, n[j], knn, d, c);
                     }
+                }
+            for (int j = 0; j < nb; ++j) {
+                const int q = qa + j;
                 const size_t o = (size_t)(q - q_base) * knn;
                 for (int k = 0; k < knn; ++k) {
-                    idx[o + k] = (k < n) ? bi[k] + 1 : q + 1;
-                    d2out[o + k] = (k < n) ? bd[k] : ORC_SINGLE_INF;
+                    idx[o + k] = (k < n[j]) ? bi[(size_t)j * knn + k] + 1 : q + 1;
+                    d2out[o + k] = (k < n[j]) ? bd[(size_t)j * knn + k] : ORC_SINGLE_INF;
                 }
             }
-            free(bd); free(bi);
         }
+        free(bd); free(bi); free(aT);
     }
+    free(B.off);
 }
 
 /* Nearest candidate not masked by R[c] <= R[q] (the search_delta_drift
@@ -667,25 +793,45 @@ void orc_exact_delta_f32(int32_t *nn, float *d2out, const float *F, const float 
                          const int32_t *q0, const int32_t *nq, const int32_t *roff,
                          const int32_t *rs, const int32_t *rn, int nChunks, int q_base)
 {
-    for (int ch = 0; ch < nChunks; ++ch) {
-#pragma omp parallel for schedule(dynamic, 8)
-        for (int qq = 0; qq < nq[ch]; ++qq) {
-            const int q = q0[ch] + qq;
-            const float *a = F + (size_t)q * nC;
-            const float ra = R[q];
-            float best = ORC_SINGLE_INF;
-            int bi = -1;
+    orc_blocks B = plan_blocks(nq, nChunks);
+#pragma omp parallel
+    {
+        float *aT = (float *)malloc(sizeof(float) * (size_t)nC * ORC_QB);
+#pragma omp for schedule(dynamic, 4)
+        for (long w = 0; w < B.total; ++w) {
+            const int ch = block_chunk(&B, nChunks, w);
+            const int qa = q0[ch] + (int)(w - B.off[ch]) * ORC_QB;
+            const int nb = (q0[ch] + nq[ch] - qa) < ORC_QB ? (q0[ch] + nq[ch] - qa) : ORC_QB;
+            float best[ORC_QB], ra[ORC_QB], rmin = INFINITY;
+            int bi[ORC_QB], skip = 1;
+            for (int j = 0; j < nb; ++j) {
+                best[j] = ORC_SINGLE_INF;
+                bi[j] = -1;
+                ra[j] = R[qa + j];
+                if (ra[j] < rmin) rmin = ra[j];
+                if (ra[j] != ra[j]) skip = 0;     /* a NaN query masks nothing: no block-wide skip */
+            }
+            stage_f32(aT, F, qa, nb, nC);
             for (int r = roff[ch]; r < roff[ch + 1]; ++r)
                 for (int c = rs[r]; c < rs[r] + rn[r]; ++c) {
-                    if (R[c] <= ra) continue;
-                    float d = dist2_fma(F + (size_t)c * nC, a, nC);
-                    if (!(d > 0.0f) || !(d < ORC_SINGLE_INF)) continue;
-                    if (bi < 0 || d < best || (d == best && c < bi)) { best = d; bi = c; }
+                    if (skip && R[c] <= rmin) continue;       /* masked for every query of the block */
+                    float dd[ORC_QB];
+                    dist2_fma_qb(dd, F + (size_t)c * nC, aT, nC);
+                    for (int j = 0; j < nb; ++j) {
+                        if (R[c] <= ra[j]) continue;
+                        const float d = dd[j];
+                        if (!(d > 0.0f) || !(d < ORC_SINGLE_INF)) continue;
+                        if (bi[j] < 0 || d < best[j] || (d == best[j] && c < bi[j])) { best[j] = d; bi[j] = c; }
+                    }
                 }
-            nn[q - q_base] = (bi < 0 ? q : bi) + 1;
-            d2out[q - q_base] = best;
+            for (int j = 0; j < nb; ++j) {
+                nn[qa + j - q_base] = (bi[j] < 0 ? qa + j : bi[j]) + 1;
+                d2out[qa + j - q_base] = best[j];
+            }
         }
+        free(aT);
     }
+    free(B.off);
 }
 
 /* irc_cuda_delta_drift.cu:28-131 (jrc3_cuda_delta_drift).  vnConst = {n1,

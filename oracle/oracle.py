@@ -227,7 +227,8 @@ def exact_delta_f64(F, R, plan, exclude_zero=True):
     qb, nout = int(plan["q_base"]), int(plan["n_out"])
     nn = np.zeros(nout, np.int32)
     d2 = np.full(nout, np.inf)
-    lib().orc_exact_delta_f64(_ptr(nn), _ptr(d2), _ptr(F), _ptr(_f32(R)), C.c_int(F.shape[1]),
+    R64 = np.ascontiguousarray(R, dtype=np.float64)     # an FP64 rho keeps its own order
+    lib().orc_exact_delta_f64(_ptr(nn), _ptr(d2), _ptr(F), _ptr(R64), C.c_int(F.shape[1]),
                               _ptr(q0), _ptr(nq), _ptr(roff), _ptr(rs), _ptr(rn),
                               C.c_int(len(q0)), C.c_int(qb), C.c_int(int(exclude_zero)))
     return nn, d2

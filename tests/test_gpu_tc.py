@@ -3,8 +3,9 @@
 Tolerances (the precision targets of the tensor-core form):
   * kNN recall >= 0.999 against the FP64 oracle (set overlap of the k lists);
   * rho = 1/d_knn within 1e-4 relative of the FP64 value;
-  * delta within 1e-4 relative of the FP64 value for spikes whose nearest
-    higher-rho neighbour agrees.
+  * delta within 1e-4 relative of the FP64 value (FP64 rho) on every spike,
+    a different nearest higher-rho neighbour counted as an error unless FP32
+    cannot resolve the two rho values (oracle/accuracy.py).
 Where the BF16 filter kept the true neighbours, the re-ranked lists equal the
 exact FP32 form bit for bit (same arithmetic), which is checked too.
 """
@@ -13,6 +14,7 @@ import pytest
 import torch
 
 from ironclust_gb300 import _lib, irc
+from oracle import accuracy as A
 from oracle import oracle as O
 from tests.cases import small_site
 
@@ -110,6 +112,9 @@ def test_mass_ties_take_the_exact_fallback(gpu):
 
 @pytest.mark.parametrize("case", CASES[:3] + CASES[4:])
 def test_bf16_delta_vs_fp64(gpu, case):
+    """Every spike: delta against the FP64 oracle with the FP64 rho; a
+    different nearest higher-rho neighbour is an error unless FP32 cannot
+    resolve the two rho values (oracle/accuracy.py)."""
     F, plan, _ = small_site(**case)
     if plan["n_out"] != F.shape[0]:
         pytest.skip("single-page site needed")
@@ -117,17 +122,14 @@ def test_bf16_delta_vs_fp64(gpu, case):
     P = irc.Plan(plan)
     out = irc.knn_rho_delta_site(P, Fd, knn=30, mode="bf16")
     _lib.check(_lib.lib().irc_plan_check(P.h, irc._stream()), "irc_plan_check")
-    R = out["rho"].cpu().numpy()
-    nn32, d2_32 = O.exact_delta_f32(F, R, plan)
-    assert np.mean(out["nneigh"].cpu().numpy() == nn32) >= 0.999
-    nn64, d2_64 = O.exact_delta_f64(F, R, plan)
-    agree = out["nneigh"].cpu().numpy() == nn64
-    found = np.isfinite(d2_64)
-    de = out["delta"].cpu().numpy()
-    ref = np.sqrt(d2_64) * R
-    m = agree & found
-    rel = np.abs(de[m] - ref[m]) / ref[m]
-    assert rel.max() <= 1e-4
+    got = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
+    R = got["rho"]
+    nn32, _ = O.exact_delta_f32(F, R, plan)
+    assert np.mean(got["nneigh"] == nn32) >= 0.999
+    acc = A.compare(got, A.fp64_reference(F, plan, 30))
+    assert acc["nneigh_errors"] == 0, acc
+    assert acc["delta_max_rel_err"] <= 1e-4, acc
+    assert acc["nneigh_rho_order_flips"] <= max(1, F.shape[0] // 10000), acc
 
 
 def test_profile_times_filter_and_rerank(gpu):
