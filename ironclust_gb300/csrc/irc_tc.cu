@@ -3,38 +3,50 @@
 //
 // A CTA serves one work item: up to four "slots", each a run of queries of
 // one drift chunk (128, 64 or 32 rows), packed into the 128 TMEM lanes of
-// one M=128 tile; every slot owns a share of the four 128-column TMEM
-// accumulators and its own epilogue warps, and the slots' candidate tiles
-// are issued round-robin so small chunks (a probe site has ~17 queries per
-// chunk) share a CTA without waiting on each other.  Items are ordered by
-// cost, largest first.  The BF16 (kind::f16) or FP8-e4m3 (kind::f8f6f4)
-// operand rows of irc_tc_host.cu -- 128 bytes each, so both use the same
-// swizzled layout and one MMA per 32 bytes -- make every accumulator the
-// approximate squared distance (FP8: a fixed positive multiple of it).
-// Warp roles: warp 0 issues
-// TMA loads (4-stage ring of 128-candidate tiles, four 32-row query boxes),
-// warp 1 owns TMEM and issues tcgen05.mma from one thread, warps 2-17 are
-// the epilogue: four per TMEM lane quarter, each reading 32 columns of
-// every tile of its slot.  Each slot's candidate tiles are streamed twice:
-//   pass 1  every thread folds its columns into 32 per-column minima (one
-//           FMNMX per pair, no branches); per query, the 64th smallest of the
-//           128 minima (found by a bitwise search, rounded up by < 2^-11
-//           relative) is an upper bound tau on the 64th nearest approximate
-//           distance (64 distinct candidates lie at or below it);
-//   pass 2  every thread marks the pairs at or below tau in a 32-bit mask
-//           (one compare and one predicated OR per pair) and appends only the
-//           marked candidates to its part-list in shared memory (~90 per
-//           query on random data, 64 per part; an overflowing query is
-//           finished by the exact fallback kernel).
-// Every listed candidate is then re-ranked with the reference FP32
-// arithmetic (exact), zero distances dropped, sorted by (distance, index)
-// with a warp bitonic network; candidates within 16 ulps of the k-th
-// distance are re-ordered by their FP64 distance.  The tensor cores
-// recompute each tile in pass 2 because they are otherwise idle: the kernel
-// is bound by the epilogue's instruction issue, not by the MMA.
+// one M=128 tile; every slot owns a share of the TMEM accumulators and its
+// own epilogue warps, and the slots' candidate tiles are issued round-robin
+// so small chunks (a probe site has ~17 queries per chunk) share a CTA
+// without waiting on each other.  Items are ordered by cost, largest first.
+// The BF16 (kind::f16) or FP8-e4m3 (kind::f8f6f4) operand rows of
+// irc_tc_host.cu -- 128 bytes each, so both use the same swizzled layout and
+// one MMA per 32 bytes -- make every accumulator the approximate squared
+// distance (FP8: a fixed positive multiple of it).
+//
+// A slot streams its chunk's 128-candidate tiles in units: items of one or
+// two slots use 256-wide units (two tiles, loaded by two TMA boxes into one
+// stage, one N = 256 MMA per K slice, two 256-column accumulators) -- the
+// issue cost of an MMA is the same at N = 256 as at 128, so this halves it
+// per pair -- and four-slot items 128-wide units (four accumulators, one per
+// slot).  Warp roles: warp 0 issues TMA loads (a 3- or 4-stage ring, four
+// 32-row query boxes), warp 1 owns TMEM and issues tcgen05.mma from one
+// thread, warps 2-17 are the epilogue: four per TMEM lane quarter, warp w of
+// a quarter reading columns 32w .. 32w + 31 of every 128-tile.  Each slot's
+// units are streamed twice:
+//   pass 1  every thread folds its columns into 32 per-column minima (the two
+//           tiles of a wide unit with one three-input min); per query, the
+//           64th smallest of the 128 minima (a bitwise search, rounded up by
+//           < 2^-11 relative) is an upper bound tau on the 64th nearest
+//           approximate distance (64 distinct candidates lie at or below it);
+//   pass 2  the candidates at or below tau are appended to the query's list
+//           in shared memory (~90 per query on random data, at most 192; an
+//           overflowing query is finished by the exact fallback kernel).  In
+//           the BF16 wide units the thresholds are folded into the MMA: each
+//           query's -tau goes into three spare K columns of its operand row,
+//           against 1s in the candidate rows, so the accumulators are
+//           d2 - tau and a hit is a sign bit (one funnel shift per pair);
+//           elsewhere every pair is compared with tau in the epilogue.
+// The minima partition is the same at both widths, so results never depend
+// on the width or the work layout.  Every listed candidate is then re-ranked
+// with the reference FP32 arithmetic (exact), zero distances dropped, sorted
+// by (distance, index) with a warp bitonic network; candidates within 16 ulps
+// of the k-th distance are re-ordered by their FP64 distance.  The kernel is
+// bound by its epilogue (TMEM loads, fold, compare, list appends), not by the
+// tensor pipe.
 #include <cuda.h>
+#include <cuda_bf16.h>
 
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "irc_common.cuh"
@@ -45,28 +57,52 @@
 namespace {
 
 using irc_tc::BM;
-using irc_tc::BN;
 using irc_tc::KP;
-constexpr int STAGES = 4;
 constexpr int PARTS = 4;                          // epilogue warps per TMEM lane quarter
-constexpr int PART = BN / PARTS;                  // columns of a tile per epilogue warp (32)
-constexpr int CAPP = 64;                          // list capacity per query and part
-constexpr int LROWP = CAPP + 1;                   // part-list row (u32), padded
-constexpr int BROW = BN + 1;                      // per-column minima row (f32) during the threshold step
+constexpr int PART = 32;                          // columns of a 128-tile per epilogue warp (one minimum each)
+constexpr int BROW = 128 + 1;                     // minima row of a query (f32, 4 parts x 32) in the threshold step
 constexpr int EPI_WARPS = 4 * PARTS;
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
-constexpr uint32_t TILE_BYTES = BN * KP * 2;      // 16 KB (A tile has the same size)
-constexpr int NBUF = 4;                           // TMEM accumulator buffers, split among the slots
-constexpr uint32_t TMEM_COLS = NBUF * BN;         // all 512 columns (one CTA per SM)
-constexpr size_t LIST_BYTES = (size_t)LROWP * PARTS * BM * 4;
+constexpr uint32_t A_BYTES = BM * KP * 2;         // the query tile: 128 rows x 128 bytes
+constexpr uint32_t HALF_BYTES = 128 * KP * 2;     // one 128-candidate tile
+constexpr uint32_t TMEM_COLS = 512;               // all TMEM columns (one CTA per SM)
+constexpr int LISTCAP = 192;                      // candidate-list capacity per query (the four warps' hits pooled)
+constexpr int LROW = LISTCAP + 1;                 // list row (u32), padded
+constexpr size_t LIST_BYTES = (size_t)LROW * BM * 4;
 constexpr int WARP_KEYS = 64;                     // sorted re-rank keys kept per epilogue warp
 constexpr int QROW4 = 16;                         // float4 of a staged query row (nC <= 64)
 constexpr int TAU_LOW_BIT = 12;                   // threshold search stops at this bit (2^-11 relative)
-constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + TILE_BYTES * (1 + STAGES) + LIST_BYTES +
-                              BM * 4 /*tau*/ + PARTS * BM * 4 /*counts*/ + 256;
-static_assert(PART == 32, "one TMEM load of 32 columns per warp and tile");
 static_assert((size_t)BROW * BM * 4 <= LIST_BYTES, "minima rows alias the list area");
-static_assert(SMEM_BYTES <= 232448, "shared memory budget");
+static_assert(LISTCAP <= irc_tc::LIST_MAX, "the re-rank takes every list the filter hands over");
+
+// Shapes of the filter for a unit width BN (MMA N): 256 for items of one or
+// two slots (two 256-column accumulators; the MMA issue cost per instruction
+// is the same at N = 256 as at 128, so the wider unit halves it per pair), 128
+// for four-slot items (one accumulator per slot).
+template <int BN>
+struct Tile {
+    static_assert(BN == 128 || BN == 256, "unit width");
+    static constexpr int NBUF = TMEM_COLS / BN;   // accumulator buffers, split among the slots
+    static constexpr int STAGES = BN == 256 ? 3 : 4;
+    static constexpr uint32_t STAGE_BYTES = BN * KP * 2;
+    static constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + A_BYTES + (size_t)STAGE_BYTES * STAGES + LIST_BYTES +
+                                         BM * 4 /*tau*/ + BM * 4 /*counts*/ + 256;
+    static_assert(SMEM_BYTES <= 232448, "shared memory budget");
+};
+
+// Work units of a slot per pass over its chunk's sequence of 128-candidate
+// tiles (nts of them).  BN = 128: one tile per unit; BN = 256: tiles 2u and
+// 2u + 1 in unit u, loaded by two TMA boxes into the halves of one 256-row
+// stage (the second absent when the count is odd).  Either way epilogue warp
+// w of a lane quarter reads columns 32w .. 32w + 31 of every 128-tile, and
+// per-column minimum i of that warp covers column 32w + i of every tile, so
+// the minima, the threshold and the candidate lists do not depend on the
+// width, nor on the work layout.
+template <int BN>
+__device__ __forceinline__ int units_per_pass(int nts)
+{
+    return BN == 256 ? (nts + 1) >> 1 : nts;
+}
 
 // Ascending bitonic sort of 32*PER keys held PER per lane (element e = lane*PER + i).
 template <class T, int PER>
@@ -292,7 +328,8 @@ __device__ __forceinline__ void slot_barrier(int slot, int nthreads)
     asm volatile("bar.sync %0, %1;" ::"r"(1 + slot), "r"(nthreads) : "memory");
 }
 
-// Cursor over the candidate tiles of one chunk: run r (absolute index), offset t.
+// Cursor over the 128-candidate tiles of one chunk: run r (absolute index), offset t.
+constexpr int TILE = 128;
 struct TileCursor {
     // run bounds of the current run (rs, rn) and of the next one (ns, nn),
     // loaded one run ahead so the loads are in flight while the current
@@ -315,8 +352,8 @@ struct TileCursor {
     __device__ __forceinline__ void next(const irc::PlanDev &p, int &row0, int &ncol)
     {
         row0 = rs + t;
-        ncol = min(BN, rn - t);
-        t += BN;
+        ncol = min(TILE, rn - t);
+        t += TILE;
         if (t >= rn) {                                // next run; wraps for the second pass
             t = 0;
             r = after(r);
@@ -333,21 +370,168 @@ __device__ __forceinline__ int chunk_tiles(const irc::PlanDev &p, int chunk)
 {
     if (chunk < 0) return 0;
     int n = 0;
-    for (int r = __ldg(p.roff + chunk); r < __ldg(p.roff + chunk + 1); ++r) n += (__ldg(p.rn + r) + BN - 1) / BN;
+    for (int r = __ldg(p.roff + chunk); r < __ldg(p.roff + chunk + 1); ++r) n += (__ldg(p.rn + r) + TILE - 1) / TILE;
     return n;
 }
 
-// Epilogue of one warp: lane quarter `quarter` (the TMEM lanes it may read),
-// 32 columns `part` of every tile of its slot.  Each slot's epilogue warps
-// synchronise only among themselves (named barrier 1 + slot).
+// Pass 1 of one warp and 128-tile (BN = 128): fold its 32 columns (taddr:
+// the first) into the per-column minima; lim = valid columns of the 32.
+__device__ __forceinline__ void fold32(uint32_t taddr, int lim, float (&bm)[PART])
+{
+    uint32_t x[16], y[16];
+    sm100::tmem_ld16_nowait(taddr, x);
+    sm100::tmem_ld16_nowait(taddr + 16, y);
+    sm100::tmem_wait_ld(x, y);
+    if (lim >= 32) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            bm[i] = fminf(bm[i], __uint_as_float(x[i]));
+            bm[16 + i] = fminf(bm[16 + i], __uint_as_float(y[i]));
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            if (i < lim) bm[i] = fminf(bm[i], __uint_as_float(x[i]));
+            if (16 + i < lim) bm[16 + i] = fminf(bm[16 + i], __uint_as_float(y[i]));
+        }
+    }
+}
+
+// Pass 1 of one warp and 256-wide unit: its 32 columns of both 128-tiles
+// (ta, tb: the first column of each; la, lb: valid columns) folded into the
+// same minima with three-input mins.
+__device__ __forceinline__ void fold2x32(uint32_t ta, int la, uint32_t tb, int lb, float (&bm)[PART])
+{
+    const float inf = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {                 // minima 16r .. 16r + 15
+        uint32_t x[16], y[16];
+        sm100::tmem_ld16_nowait(ta + 16 * r, x);
+        sm100::tmem_ld16_nowait(tb + 16 * r, y);
+        sm100::tmem_wait_ld(x, y);
+        if (la >= 32 && lb >= 32) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                bm[16 * r + i] = sm100::fmin3(bm[16 * r + i], __uint_as_float(x[i]), __uint_as_float(y[i]));
+        } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                bm[16 * r + i] = sm100::fmin3(bm[16 * r + i], 16 * r + i < la ? __uint_as_float(x[i]) : inf,
+                                              16 * r + i < lb ? __uint_as_float(y[i]) : inf);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned lim_mask(int lim)
+{
+    return lim >= 32 ? 0xffffffffu : lim <= 0 ? 0u : (1u << lim) - 1u;
+}
+
+// Pass 2 of one warp and 128-tile: the mask of its 32 columns at or below
+// tau, limited to the lim valid columns.
+__device__ __forceinline__ unsigned mark32(uint32_t taddr, int lim, float tau)
+{
+    uint32_t x[16], y[16];
+    sm100::tmem_ld16_nowait(taddr, x);
+    sm100::tmem_ld16_nowait(taddr + 16, y);
+    sm100::tmem_wait_ld(x, y);
+    // four independent partial masks: short dependency chains
+    unsigned a0 = 0u, a1 = 0u, a2 = 0u, a3 = 0u;
+#pragma unroll
+    for (int i = 0; i < 16; i += 2) {
+        if (__uint_as_float(x[i]) <= tau) a0 |= 1u << i;
+        if (__uint_as_float(x[i + 1]) <= tau) a1 |= 1u << (i + 1);
+        if (__uint_as_float(y[i]) <= tau) a2 |= 1u << (16 + i);
+        if (__uint_as_float(y[i + 1]) <= tau) a3 |= 1u << (17 + i);
+    }
+    return ((a0 | a1) | (a2 | a3)) & lim_mask(lim);
+}
+
+// Bit c of the result = sign bit of v[c], one funnel shift per value in two
+// independent chains.
+__device__ __forceinline__ unsigned signs16(const uint32_t (&v)[16])
+{
+    unsigned c0 = 0u, c1 = 0u;                    // values 0-7, 8-15
+#pragma unroll
+    for (int i = 7; i >= 0; --i) {
+        c0 = __funnelshift_l(v[i], c0, 1);
+        c1 = __funnelshift_l(v[8 + i], c1, 1);
+    }
+    return c0 | (c1 << 8);
+}
+
+// Pass 2 with the threshold folded into the MMA (accumulators d2 - tau) of
+// one warp and 256-wide unit: the masks of its 32 columns of each tile with a
+// negative accumulator, limited to the valid columns.
+__device__ __forceinline__ void mark2x32_signs(uint32_t ta, int la, uint32_t tb, int lb, unsigned &ma, unsigned &mb)
+{
+    unsigned a[2], b[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {                 // columns 16r .. 16r + 15 of both tiles
+        uint32_t x[16], y[16];
+        sm100::tmem_ld16_nowait(ta + 16 * r, x);
+        sm100::tmem_ld16_nowait(tb + 16 * r, y);
+        sm100::tmem_wait_ld(x, y);
+        a[r] = signs16(x);
+        b[r] = signs16(y);
+    }
+    ma = (a[0] | (a[1] << 16)) & lim_mask(la);
+    mb = (b[0] | (b[1] << 16)) & lim_mask(lb);
+}
+
+// The pass-2 threshold of query row `row` into the query tile in shared
+// memory: -tau' split exactly into three BF16 terms at K positions tau_k ..
+// tau_k + 2, against 1, 1, 1 in every candidate row, so the pass-2
+// accumulators are d2 - tau'.  tau' = tau (1 + 2^-10), capped at 1e30: the
+// small margin keeps every candidate at or below tau negative whatever the
+// rounding of the extra terms.  The tile is 128-byte swizzled: the 16-byte
+// piece c of row r sits at piece c ^ (r % 8).
+__device__ __forceinline__ void put_tau(uint8_t *sA, int row, int tau_k, float tau)
+{
+    const float x = -fminf(tau * (1.0f + 0x1p-10f), 1e30f);
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h);
+    const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+    const __nv_bfloat16 v[3] = {h, m, l};
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        const int k = tau_k + t;
+        __nv_bfloat16 *dst = reinterpret_cast<__nv_bfloat16 *>(sA + (size_t)row * 128 +
+                                                               (((k >> 3) ^ (row & 7)) << 4) + (k & 7) * 2);
+        *dst = v[t];
+    }
+}
+
+// Append the hits of a 32-column mask (columns c0 + bit) to the query's
+// pooled list (its four epilogue warps share it): one shared-memory atomic
+// reserves the room; entries past LISTCAP are dropped, and a count past it
+// sends the query to the exact fallback.
+__device__ __forceinline__ void append_hits(uint32_t *lrow, int *cnt, unsigned m, uint32_t c0)
+{
+    int e = atomicAdd(cnt, __popc(m));
+    while (m) {
+        const int jj = __ffs(m) - 1;
+        m &= m - 1u;
+        if (e < LISTCAP) lrow[e] = c0 + (uint32_t)jj;
+        ++e;
+    }
+}
+
+// Epilogue of one warp: lane quarter `quarter` (the TMEM lanes it may read)
+// and part `part` (columns 32 * part .. 32 * part + 31 of every 128-tile of
+// its slot).  Each slot's epilogue warps synchronise only among themselves
+// (named barrier 1 + slot).
+template <int BN, bool TAU>
 __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::TcItem &it, const int (&nt)[4], int qps,
-                                         int bps, uint32_t tmem, uint32_t *lists, float *sTau, int *sCnt,
-                                         uint64_t *acc_full, uint64_t *acc_empty, volatile int *abort_flag,
-                                         const irc_tc::ListOut &lo, int *scratch, int warp, int lane)
+                                         int bps, uint32_t tmem, uint8_t *sA, int tau_k, uint32_t *lists, float *sTau,
+                                         int *sCnt, uint64_t *acc_full, uint64_t *acc_empty, uint64_t *tau_ready,
+                                         volatile int *abort_flag, const irc_tc::ListOut &lo, int *scratch, int warp,
+                                         int lane)
 {
     const int ew = warp - 2;                      // 0..15
     const int quarter = warp & 3;                 // TMEM lane quarter this warp may access
-    const int part = ew >> 2;                     // which 32 columns of every tile
+    const int part = ew >> 2;                     // its 32 columns of every 128-tile
     const int s = quarter / qps;                  // slot of this lane quarter
     const int qrow = (quarter % qps) * 32;        // first row of this quarter inside its slot
     const int nq_s = it.chunk[s] >= 0 ? it.nq[s] : 0;
@@ -356,34 +540,40 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
     const int row = quarter * 32 + lane;
     const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + part * PART;
     const bool active = qrow < nq_s;              // warp-uniform: any valid query in this quarter
+    const int lb = bps == 4 ? 2 : bps == 2 ? 1 : 0;   // unit k is phase k / bps of its buffer's barriers
+    const int U = units_per_pass<BN>(nts);
     bool ok = true;
     TileCursor cur;
     if (nts) cur.reset(p, it.chunk[s]);
 
-    // pass 1: per-column minima of this part
+    // Unit k: first row and valid count of this warp's columns in the unit's
+    // tile(s) (b: the second 128-tile of a 256-wide unit, none: nb = 0).
+    auto unit = [&](int k, int &ra, int &na, int &rb, int &nb) {
+        ra = na = rb = nb = 0;
+        cur.next(p, ra, na);
+        na -= part * PART;
+        if (BN == 256 && 2 * (k % U) + 1 < nts) {
+            cur.next(p, rb, nb);
+            nb -= part * PART;
+        }
+    };
+
+    // pass 1: per-column minima of this warp's columns
     float bm[PART];
 #pragma unroll
     for (int c = 0; c < PART; ++c) bm[c] = __int_as_float(0x7f800000);
-    int bj = 0, use = 0;                          // tile j of this slot: buffer s*bps + bj, use count
-    for (int j = 0; j < nts && ok; ++j) {
-        const int b = s * bps + bj;
-        const uint32_t par = use & 1;
-        if (++bj == bps) { bj = 0; ++use; }
-        int row0, ncol;
-        cur.next(p, row0, ncol);
-        if (!(ok = sm100::mbar_wait(&acc_full[b], par, abort_flag))) break;
+    for (int k = 0; k < U && ok; ++k) {
+        int ra, na, rb, nb;
+        unit(k, ra, na, rb, nb);
+        const int b = s * bps + (k & (bps - 1));
+        if (!(ok = sm100::mbar_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
         sm100::tc_fence_after();
-        const int lim = ncol - part * PART;                   // valid columns in this part
-        if (active && lim > 0) {
-            float v[32];
-            sm100::tmem_ld32(tbase + b * BN, v);
-            if (lim >= 32) {
-#pragma unroll
-                for (int jj = 0; jj < 32; ++jj) bm[jj] = fminf(bm[jj], v[jj]);
+        if (active) {
+            if constexpr (BN == 256) {
+                // either tile may be the short one (the first when it ends a run)
+                if (na > 0 || nb > 0) fold2x32(tbase + b * BN, na, tbase + b * BN + 128, nb, bm);
             } else {
-#pragma unroll
-                for (int jj = 0; jj < 32; ++jj)
-                    if (jj < lim) bm[jj] = fminf(bm[jj], v[jj]);
+                if (na > 0) fold32(tbase + b * BN, na, bm);
             }
         }
         sm100::tc_fence_before();
@@ -392,11 +582,12 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
     }
     // threshold: 64th smallest of the 128 column minima of every query; the
     // minima rows of a quarter alias that quarter's own list rows
-    float *qarea = reinterpret_cast<float *>(lists + (size_t)quarter * 32 * PARTS * LROWP);
+    float *qarea = reinterpret_cast<float *>(lists + (size_t)quarter * 32 * LROW);
     {
         float *brow = qarea + lane * BROW + part * PART;
 #pragma unroll
         for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
+        if (part == 0) sCnt[row] = 0;             // list counts of pass 2 (ordered by the barriers below)
         slot_barrier(s, slot_threads);
         // The warp's 8 rows at once (independent chains): a bitwise search,
         // from the top, of the largest t with fewer than 64 minima below it,
@@ -433,62 +624,49 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
         slot_barrier(s, slot_threads);     // minima rows are read; the list rows may be written
     }
     const float tau = sTau[row];
+    if (TAU && part == 0) {
+        // the thresholds into the query tile; visible to the tensor core
+        // (async proxy) before the MMA thread, released by tau_ready, issues
+        // the slot's pass-2 MMAs
+        put_tau(sA, row, tau_k, tau);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) sm100::mbar_arrive(&tau_ready[s]);
+    }
     // pass 2: collect the candidates at or below tau
-    uint32_t *lrow = lists + ((size_t)row * PARTS + part) * LROWP;
-    int cnt = 0;
-    bool ovf = false;
-    for (int j = nts; j < 2 * nts && ok; ++j) {
-        const int b = s * bps + bj;
-        const uint32_t par = use & 1;
-        if (++bj == bps) { bj = 0; ++use; }
-        int row0, ncol;
-        cur.next(p, row0, ncol);
-        if (!(ok = sm100::mbar_wait(&acc_full[b], par, abort_flag))) break;
+    uint32_t *lrow = lists + (size_t)row * LROW;
+    for (int k = U; k < 2 * U && ok; ++k) {
+        int ra, na, rb, nb;
+        unit(k, ra, na, rb, nb);
+        const int b = s * bps + (k & (bps - 1));
+        if (!(ok = sm100::mbar_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
         sm100::tc_fence_after();
-        const int lim = ncol - part * PART;
-        if (active && lim > 0) {
-            float v[32];
-            sm100::tmem_ld32(tbase + b * BN, v);
-            // four independent partial masks: short dependency chains
-            unsigned mq[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-            for (int jj = 0; jj < 32; ++jj)
-                if (v[jj] <= tau) mq[jj & 3] |= 1u << jj;
-            unsigned m = (mq[0] | mq[1]) | (mq[2] | mq[3]);
-            if (lim < 32) m &= (1u << lim) - 1u;
-            if (cnt + __popc(m) > CAPP) { ovf = true; m = 0; }
-            const uint32_t c0 = (uint32_t)(row0 + part * PART);
-            while (m) {
-                const int jj = __ffs(m) - 1;
-                m &= m - 1u;
-                lrow[cnt++] = c0 + (uint32_t)jj;
+        if (active && (na > 0 || nb > 0)) {
+            unsigned ma = 0u, mb = 0u;
+            if constexpr (BN == 256 && TAU) {
+                mark2x32_signs(tbase + b * BN, na, tbase + b * BN + 128, nb, ma, mb);
+            } else {
+                if (na > 0) ma = mark32(tbase + b * BN, na, tau);
+                if (BN == 256 && nb > 0) mb = mark32(tbase + b * BN + 128, nb, tau);
             }
+            if (ma) append_hits(lrow, sCnt + row, ma, (uint32_t)(ra + part * PART));
+            if (mb) append_hits(lrow, sCnt + row, mb, (uint32_t)(rb + part * PART));
         }
         sm100::tc_fence_before();
         __syncwarp();
         if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
     }
-    sCnt[row * PARTS + part] = ovf ? -1 : cnt;
     slot_barrier(s, slot_threads);
     // Hand the lists to the re-rank kernel: this warp packs 8 of its
     // quarter's queries (query L in lane L) into one bump allocation and
-    // records (offset, length) per query; an overflowed part-list, a list
-    // longer than LIST_MAX or a full list area sends the query to the exact
-    // fallback instead.
+    // records (offset, length) per query; a list past LISTCAP or a full list
+    // area sends the query to the exact fallback instead.
     if (!__all_sync(0xffffffffu, ok)) return;
     constexpr int RL = 32 / PARTS;
     int cL = -1;                                  // -1: no query in this lane, -2: to the fallback
     if (lane < RL && qrow + part * RL + lane < nq_s) {
-        const int rowL = quarter * 32 + part * RL + lane;
-        int t = 0;
-        bool over = false;
-#pragma unroll
-        for (int u = 0; u < PARTS; ++u) {
-            const int c = sCnt[rowL * PARTS + u];
-            over |= c < 0;
-            t += c;
-        }
-        cL = (over || t > irc_tc::LIST_MAX) ? -2 : t;
+        const int t = sCnt[quarter * 32 + part * RL + lane];
+        cL = t > LISTCAP ? -2 : t;
     }
     const unsigned len = cL > 0 ? (unsigned)cL : 0u;
     unsigned incl = len;
@@ -519,47 +697,35 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
         const int n = __shfl_sync(0xffffffffu, cL, L);
         const unsigned off = base + __shfl_sync(0xffffffffu, incl - len, L);
         if (n <= 0) continue;                     // warp-uniform
-        const int rowL = quarter * 32 + part * RL + L;
-        const int c0 = sCnt[rowL * PARTS + 0], c1 = sCnt[rowL * PARTS + 1], c2 = sCnt[rowL * PARTS + 2];
-        const uint32_t *lr = lists + (size_t)rowL * PARTS * LROWP;
-        for (int e = lane; e < n; e += 32) {
-            int pp = 0, r = e;
-            if (r >= c0) {
-                r -= c0;
-                pp = 1;
-                if (r >= c1) {
-                    r -= c1;
-                    pp = 2;
-                    if (r >= c2) { r -= c2; pp = 3; }
-                }
-            }
-            lo.lists[off + e] = lr[pp * LROWP + r];
-        }
+        const uint32_t *lr = lists + (size_t)(quarter * 32 + part * RL + L) * LROW;
+        for (int e = lane; e < n; e += 32) lo.lists[off + e] = lr[e];
     }
 }
 
 // TMA producer (one thread): the four 32-row query boxes, then the slots'
-// candidate tiles round-robin, each slot's sequence twice (both passes).
-template <int NS>
+// units round-robin, each slot's sequence twice (both passes).  A unit's
+// 128-candidate tiles land in consecutive 128-row halves of its stage.
+template <int BN, int NS>
 __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMap &tmC, const irc::PlanDev &p,
                                         const irc_tc::TcItem &it, const int (&nt)[4], uint8_t *sA, uint8_t *sB,
                                         uint64_t *full, uint64_t *empty, uint64_t *a_full, volatile int *abort_flag)
 {
+    using T = Tile<BN>;
     constexpr int QPS = 4 / NS;
     sm100::prefetch_tmap(&tmQ);
     sm100::prefetch_tmap(&tmC);
-    sm100::mbar_arrive_expect_tx(a_full, TILE_BYTES);
+    sm100::mbar_arrive_expect_tx(a_full, A_BYTES);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int s = q / QPS;
         const int row0 = it.chunk[s] >= 0 ? it.qs[s] + (q % QPS) * 32 : 0;
-        sm100::tma_load_2d(&tmQ, a_full, sA + q * (TILE_BYTES / 4), 0, row0);
+        sm100::tma_load_2d(&tmQ, a_full, sA + q * (A_BYTES / 4), 0, row0);
     }
     TileCursor cur[NS];
-    int n2[NS];
+    int U[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
-        n2[s] = 2 * nt[s];
+        U[s] = units_per_pass<BN>(nt[s]);
         if (nt[s]) cur[s].reset(p, it.chunk[s]);
     }
     int i = 0;
@@ -568,14 +734,19 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
         bool any = false;
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-            if (ok && k < n2[s]) {
+            if (ok && k < 2 * U[s]) {
                 any = true;
-                int row0, ncol;
-                cur[s].next(p, row0, ncol);
-                const int st = i % STAGES;
-                if ((ok = sm100::mbar_wait(&empty[st], ((i / STAGES) & 1) ^ 1, abort_flag))) {
-                    sm100::mbar_arrive_expect_tx(&full[st], TILE_BYTES);
-                    sm100::tma_load_2d(&tmC, &full[st], sB + (size_t)st * TILE_BYTES, 0, row0);
+                const int u = k % U[s];
+                const int st = i % T::STAGES;
+                if ((ok = sm100::mbar_wait(&empty[st], ((i / T::STAGES) & 1) ^ 1, abort_flag))) {
+                    uint8_t *dst = sB + (size_t)st * T::STAGE_BYTES;
+                    const int nh = BN == 256 && 2 * u + 1 < nt[s] ? 2 : 1;   // 128-tiles of the unit
+                    sm100::mbar_arrive_expect_tx(&full[st], nh * HALF_BYTES);
+                    for (int h = 0; h < nh; ++h) {
+                        int row0, ncol;
+                        cur[s].next(p, row0, ncol);
+                        sm100::tma_load_2d(&tmC, &full[st], dst + h * HALF_BYTES, 0, row0);
+                    }
                     ++i;
                 }
             }
@@ -583,42 +754,50 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
         if (!any) break;
     }
     // every issued load has landed before the CTA exits
-    for (int j = (i > STAGES ? i - STAGES : 0); j < i; ++j)
-        sm100::mbar_wait(&full[j % STAGES], (j / STAGES) & 1, abort_flag);
+    for (int j = (i > T::STAGES ? i - T::STAGES : 0); j < i; ++j)
+        sm100::mbar_wait(&full[j % T::STAGES], (j / T::STAGES) & 1, abort_flag);
     sm100::mbar_wait(a_full, 0, abort_flag);
 }
 
-// MMA issuer (one thread), in the producer's order; slot s's tile k goes to
-// accumulator s*BPS + k % BPS.
-template <int NS, bool FP8>
-__device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem, uint8_t *sA, uint8_t *sB, uint64_t *full,
-                                      uint64_t *empty, uint64_t *a_full, uint64_t *acc_full, uint64_t *acc_empty,
-                                      uint64_t *mma_done, volatile int *abort_flag)
+// MMA issuer (one thread), in the producer's order; slot s's unit k goes to
+// accumulator s*BPS + k % BPS and is issued once every epilogue warp of the
+// slot released the previous unit in that buffer (k - BPS).  With TAU the
+// slot's first pass-2 unit also waits until its epilogue wrote the
+// thresholds into the query tile (tau_ready[s]).
+template <int BN, int NS, bool FP8, bool TAU>
+__device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem, uint8_t *sA,
+                                      uint8_t *sB, uint64_t *full, uint64_t *empty, uint64_t *a_full,
+                                      uint64_t *acc_full, uint64_t *acc_empty, uint64_t *tau_ready, uint64_t *mma_done,
+                                      volatile int *abort_flag)
 {
-    constexpr int BPS = NBUF / NS;
+    using T = Tile<BN>;
+    constexpr int BPS = T::NBUF / NS;
     // bf16 x bf16 (kind::f16, K = 16) or e4m3 x e4m3 (kind::f8f6f4, K = 32) -> f32;
     // either way one MMA consumes 32 bytes of every 128-byte operand row
     constexpr uint32_t idesc = FP8 ? sm100::idesc_make(BM, BN, 0, 0) : sm100::idesc_make(BM, BN, 1, 1);
     if (sm100::mbar_wait(a_full, 0, abort_flag)) {
         sm100::tc_fence_after();
         const uint64_t adesc = sm100::sdesc_sw128(sm100::smem_u32(sA));
-        int n2[NS];
+        int U[NS];
 #pragma unroll
-        for (int s = 0; s < NS; ++s) n2[s] = 2 * nt[s];
+        for (int s = 0; s < NS; ++s) U[s] = units_per_pass<BN>(nt[s]);
         int i = 0;
         bool ok = true;
         for (int k = 0; ok; ++k) {
             bool any = false;
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
-                if (ok && k < n2[s]) {
+                if (ok && k < 2 * U[s]) {
                     any = true;
-                    const int b = s * BPS + k % BPS, u = k / BPS, st = i % STAGES;
-                    ok = sm100::mbar_wait(&acc_empty[b], (u & 1) ^ 1, abort_flag) &&
-                         sm100::mbar_wait(&full[st], (i / STAGES) & 1, abort_flag);
+                    const int b = s * BPS + k % BPS, st = i % T::STAGES;
+                    ok = (k < BPS || sm100::mbar_wait(&acc_empty[b], ((k - BPS) / BPS) & 1, abort_flag)) &&
+                         sm100::mbar_wait(&full[st], (i / T::STAGES) & 1, abort_flag) &&
+                         // the slot's thresholds are in the query tile before its pass 2
+                         (!TAU || k != U[s] || sm100::mbar_wait(&tau_ready[s], 0, abort_flag));
                     if (ok) {
                         sm100::tc_fence_after();
-                        const uint64_t bdesc = sm100::sdesc_sw128(sm100::smem_u32(sB + (size_t)st * TILE_BYTES));
+                        const uint64_t bdesc =
+                            sm100::sdesc_sw128(sm100::smem_u32(sB + (size_t)st * T::STAGE_BYTES));
 #pragma unroll
                         for (int kk = 0; kk < KP / 16; ++kk)
                             if (kk >= nk)
@@ -641,39 +820,47 @@ __device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem,
     sm100::mbar_wait(mma_done, 0, abort_flag);
 }
 
-template <bool FP8>
+// The filter over the work items of one unit width (items of one or two slots
+// at BN = 256, four-slot items at BN = 128); TAU: pass 2 reads the signs of
+// d2 - tau (the thresholds written into the query tile at K position tau_k),
+// else it compares d2 with tau in the epilogue.
+template <bool FP8, int BN, bool TAU>
 __global__ void __launch_bounds__(THREADS, 1)
 k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
-              const irc_tc::TcItem *__restrict__ items, int nk, irc_tc::ListOut lo, int *__restrict__ scratch)
+         const irc_tc::TcItem *__restrict__ items, int nk, int tau_k, irc_tc::ListOut lo, int *__restrict__ scratch)
 {
+    using T = Tile<BN>;
     extern __shared__ unsigned char smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *sA = base;
-    uint8_t *sB = base + TILE_BYTES;
-    uint32_t *lists = reinterpret_cast<uint32_t *>(sB + STAGES * TILE_BYTES);        // [BM][PARTS][LROWP]
-    float *sTau = reinterpret_cast<float *>(lists + (size_t)LROWP * PARTS * BM);     // [BM]
-    int *sCnt = reinterpret_cast<int *>(sTau + BM);                                  // [BM][PARTS], -1 = overflow
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sCnt + PARTS * BM);
-    uint64_t *full = bars, *empty = bars + STAGES, *a_full = bars + 2 * STAGES;
-    uint64_t *acc_full = a_full + 1, *acc_empty = acc_full + NBUF, *mma_done = acc_empty + NBUF;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+    uint8_t *sB = base + A_BYTES;
+    uint32_t *lists = reinterpret_cast<uint32_t *>(sB + T::STAGES * T::STAGE_BYTES);   // [BM][LROW]
+    float *sTau = reinterpret_cast<float *>(lists + (size_t)LROW * BM);              // [BM]
+    int *sCnt = reinterpret_cast<int *>(sTau + BM);                                  // [BM] list counts
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sCnt + BM);
+    uint64_t *full = bars, *empty = bars + T::STAGES, *a_full = bars + 2 * T::STAGES;
+    uint64_t *acc_full = a_full + 1, *acc_empty = acc_full + T::NBUF;
+    uint64_t *mma_done = acc_empty + T::NBUF;
+    uint64_t *tau_ready = mma_done + 1;                                              // [4], one per slot
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tau_ready + 4);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const irc_tc::TcItem it = items[blockIdx.x];
-    const int nslot = it.nslot, qps = 4 / nslot, bps = NBUF / nslot;
+    const int nslot = it.nslot, qps = 4 / nslot, bps = T::NBUF / nslot;
     int nt[4];
 #pragma unroll
-    for (int s = 0; s < 4; ++s) nt[s] = s < nslot ? chunk_tiles(p, it.chunk[s]) : 0;
+    for (int s = 0; s < 4; ++s) nt[s] = s < nslot ? chunk_tiles(p, it.chunk[s]) : 0;    // 128-tiles
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) { sm100::mbar_init(&full[s], 1); sm100::mbar_init(&empty[s], 1); }
+        for (int s = 0; s < T::STAGES; ++s) { sm100::mbar_init(&full[s], 1); sm100::mbar_init(&empty[s], 1); }
         sm100::mbar_init(a_full, 1);
-        for (int b = 0; b < NBUF; ++b) {
+        for (int b = 0; b < T::NBUF; ++b) {
             sm100::mbar_init(&acc_full[b], 1);
-            sm100::mbar_init(&acc_empty[b], PARTS * qps);      // the owning slot's epilogue warps
+            sm100::mbar_init(&acc_empty[b], PARTS * qps);       // the slot's epilogue warps
         }
         sm100::mbar_init(mma_done, 1);
+        for (int s = 0; s < 4; ++s) sm100::mbar_init(&tau_ready[s], qps);   // the slot's quarters' writers
         *abort_flag = 0;
         sm100::fence_mbar_init();
     }
@@ -685,20 +872,40 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
 
     if (warp == 0) {
         if (lane == 0) {
-            if (nslot == 1) produce<1>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
-            else if (nslot == 2) produce<2>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
-            else produce<4>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+            if constexpr (BN == 256) {                // one or two slots
+                if (nslot == 1) produce<BN, 1>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+                else produce<BN, 2>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+            } else {
+                if (nslot == 1) produce<BN, 1>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+                else if (nslot == 2) produce<BN, 2>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+                else produce<BN, 4>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            if (nslot == 1) issue<1, FP8>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
-            else if (nslot == 2) issue<2, FP8>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
-            else issue<4, FP8>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, mma_done, abort_flag);
+            if constexpr (BN == 256) {
+                if (nslot == 1)
+                    issue<BN, 1, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready, mma_done,
+                                      abort_flag);
+                else
+                    issue<BN, 2, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready, mma_done,
+                                      abort_flag);
+            } else {
+                if (nslot == 1)
+                    issue<BN, 1, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready,
+                                           mma_done, abort_flag);
+                else if (nslot == 2)
+                    issue<BN, 2, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready,
+                                           mma_done, abort_flag);
+                else
+                    issue<BN, 4, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready,
+                                           mma_done, abort_flag);
+            }
         }
         __syncwarp();
     } else {
-        epilogue(p, it, nt, qps, bps, tmem, lists, sTau, sCnt, acc_full, acc_empty, abort_flag, lo, scratch, warp,
-                 lane);
+        epilogue<BN, TAU>(p, it, nt, qps, bps, tmem, sA, tau_k, lists, sTau, sCnt, acc_full, acc_empty, tau_ready, abort_flag,
+                     lo, scratch, warp, lane);
     }
     sm100::tc_fence_before();
     __syncthreads();
@@ -762,25 +969,55 @@ static cudaEvent_t *profile_slot()
     return &g_prof_ev[3 * g_prof_used++];
 }
 
+template <bool FP8, int BN, bool TAU>
+static int launch_filter(const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const irc_tc::TcItem *items,
+                         int n_items, int nk, int tau_k, const ListOut &lo, cudaStream_t s)
+{
+    if (n_items <= 0) return IRC_OK;
+    auto kern = k_knn_tc<FP8, BN, TAU>;
+    const int smem = (int)Tile<BN>::SMEM_BYTES;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): smem attribute");
+    kern<<<n_items, THREADS, smem, s>>>(mq, mc, pl->dev, items, nk, tau_k, lo, pl->scratch);
+    IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
+    return IRC_OK;
+}
+
 int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F,
                   const float4 *Fp, int nC, int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn,
                   const ListOut &lo, cudaStream_t s)
 {
-    auto kern = fp8 ? k_knn_tc<true> : k_knn_tc<false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
-    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): smem attribute");
     const int n_out = pl->dev.n_out;
-    e = cudaMemsetAsync(lo.qinfo, 0xff, (size_t)n_out * sizeof(int2), s);          // (-1, -1): no list
+    cudaError_t e = cudaMemsetAsync(lo.qinfo, 0xff, (size_t)n_out * sizeof(int2), s);   // (-1, -1): no list
     if (e == cudaSuccess) e = cudaMemsetAsync(lo.count, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): memset");
-    // MMAs per tile: only the 32-byte K slices that hold data (nC features
-    // plus 6 BF16 / 12 FP8 norm entries); the rest of each row is zero
-    const int used = fp8 ? nC + 12 : 2 * (nC + 6);
+    // BF16: the pass-2 thresholds go into K positions nC + 6 .. nC + 8 of the
+    // query rows when they fit (else, and for FP8, pass 2 compares in the
+    // epilogue).  MMAs per unit: only the 32-byte K slices that hold data
+    // (nC features, 6 BF16 / 12 FP8 norm entries, the threshold terms).
+    const int tau_k = (!fp8 && nC + 9 <= KP) ? nC + 6 : -1;
+    const int used = fp8 ? nC + 12 : 2 * (nC + (tau_k >= 0 ? 9 : 6));
     const int nk = (used + 31) / 32;
     cudaEvent_t *ev = profile_slot();
     if (ev) cudaEventRecord(ev[0], s);
-    kern<<<pl->n_tc_items, THREADS, SMEM_BYTES, s>>>(mq, mc, pl->dev, pl->tc_items, nk, lo, pl->scratch);
-    IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
+    // items of one or two slots on 256-candidate units, then four-slot items on 128
+    const int nw = pl->n_tc_wide, nn = pl->n_tc_items - pl->n_tc_wide;
+    // Four-slot items (small chunks) keep the compare in the epilogue: their
+    // CTAs are short, and waiting for the thresholds before the pass-2 MMAs
+    // would put the threshold step on their critical path.  The width never
+    // changes the results.
+    using yes = std::true_type;
+    using no = std::false_type;
+    auto run = [&](auto tau_c) {
+        constexpr bool T = decltype(tau_c)::value;
+        int r = fp8 ? launch_filter<true, 256, false>(mq, mc, pl, pl->tc_items, nw, nk, tau_k, lo, s)
+                    : launch_filter<false, 256, T>(mq, mc, pl, pl->tc_items, nw, nk, tau_k, lo, s);
+        if (r != IRC_OK) return r;
+        return fp8 ? launch_filter<true, 128, false>(mq, mc, pl, pl->tc_items + nw, nn, nk, tau_k, lo, s)
+                   : launch_filter<false, 128, false>(mq, mc, pl, pl->tc_items + nw, nn, nk, tau_k, lo, s);
+    };
+    const int rc = tau_k >= 0 ? run(yes{}) : run(no{});
+    if (rc != IRC_OK) return rc;
     if (ev) cudaEventRecord(ev[1], s);
     k_rerank<<<(n_out + RR_WARPS - 1) / RR_WARPS, 32 * RR_WARPS, 0, s>>>(
         lo.qinfo, lo.lists, n_out, pl->dev.q_base, F, Fp, nC, knn, vrKnn, rho, miKnn, d2Knn, pl->scratch);

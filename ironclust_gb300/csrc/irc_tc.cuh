@@ -7,7 +7,6 @@
 namespace irc_tc {
 
 constexpr int BM = 128;          // queries per CTA (TMEM lanes)
-constexpr int BN = 128;          // candidates per tile (TMEM columns)
 constexpr int KP = 64;           // padded feature dimension (bf16 elements, one 128-byte row)
 constexpr int KNN_MAX = 32;      // largest knn served (candidate lists hold >= 64 for the re-rank)
 constexpr int LIST_MAX = 256;    // longest candidate list re-ranked (else: the exact fallback)
@@ -54,6 +53,9 @@ inline ListOut list_area(void *base, long long n_out)
     return lo;
 }
 
+// The filter (items of one or two slots on 256-candidate units, four-slot
+// items on 128-candidate units; mc is the candidate-row map with 128-row
+// boxes) and the re-rank, on stream s.
 int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F,
                   const float4 *Fp, int nC, int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn,
                   const ListOut &lo, cudaStream_t s);

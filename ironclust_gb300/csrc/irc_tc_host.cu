@@ -2,12 +2,14 @@
 //
 // Operand rows.  Every spike is stored twice in BF16, padded to K = 64 (one
 // 128-byte swizzle row):
-//     query row     [ -2*a_1 .. -2*a_D,  na_h, na_m, na_l,  1, 1, 1,  0 ... ]
-//     candidate row [    b_1 ..    b_D,     1,    1,    1, nb_h, nb_m, nb_l, 0 ... ]
+//     query row     [ -2*a_1 .. -2*a_D,  na_h, na_m, na_l,  1, 1, 1,  0, 0, 0,  0 ... ]
+//     candidate row [    b_1 ..    b_D,     1,    1,    1, nb_h, nb_m, nb_l, 1, 1, 1, 0 ... ]
 // where a, b are the BF16-rounded features and na = |a|^2 (FP32, from the
 // rounded values) split exactly into three BF16 terms, so one K = 64
 // contraction yields |a|^2 + |b|^2 - 2 a.b = |a - b|^2 of the rounded
-// features, accumulated in FP32.
+// features, accumulated in FP32.  The filter's second pass writes a query's
+// threshold, -tau split into three BF16 terms, into the three zeros of its
+// row in shared memory (irc_tc.cu): its accumulators are then d2 - tau.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -165,6 +167,8 @@ k_prep(const float *__restrict__ F, int lo, int n, int nC, const float *__restri
                     } else if (k < nC + 6) {
                         vq = one;
                         vc = (k == nC + 3) ? h : (k == nC + 4) ? m : l;
+                    } else if (k < nC + 9) {
+                        vc = one;                  // against the query's pass-2 threshold terms
                     }
                     wq[e] = vq;
                     wc[e] = vc;
@@ -323,7 +327,7 @@ int irc_site_knn_tc(irc_plan *pl, const float *F, int nC, int knn, int mode, flo
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core) prep");
     CUtensorMap mq, mc;
     if ((rc = make_map(&mq, fq, nF, 32, fp8)) != IRC_OK) return rc;       // 32 query rows per lane quarter
-    if ((rc = make_map(&mc, fc, nF, irc_tc::BN, fp8)) != IRC_OK) return rc;
+    if ((rc = make_map(&mc, fc, nF, 128, fp8)) != IRC_OK) return rc;     // 128-row candidate tiles
     rc = irc_tc::launch_knn_tc(fp8, mq, mc, pl, F, (const float4 *)fp, nC, knn, vrKnn, rho, miKnn, d2Knn, lo, s);
     if (rc != IRC_OK) return rc;
     return irc_exact_overflow_drain(pl, F, nC, knn, vrKnn, rho, miKnn, d2Knn, s);
