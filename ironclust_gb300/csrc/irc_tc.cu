@@ -24,11 +24,12 @@
 // units are streamed twice:
 //   pass 1  every thread folds its columns into 32 per-column minima (the two
 //           tiles of a wide unit with one three-input min); per query, the
-//           64th smallest of the 128 minima (a bitwise search, rounded up by
-//           < 2^-11 relative) is an upper bound tau on the 64th nearest
-//           approximate distance (64 distinct candidates lie at or below it);
+//           r-th smallest of the 128 minima (r = 48 for BF16, 64 for FP8; a
+//           bitwise search, rounded up by < 2^-11 relative) is an upper bound
+//           tau on the r-th nearest approximate distance (r distinct
+//           candidates lie at or below it, against knn <= 32);
 //   pass 2  the candidates at or below tau are appended to the query's list
-//           in shared memory (~90 per query on random data, at most 192; an
+//           in shared memory (~70 per query on random data, at most 192; an
 //           overflowing query is finished by the exact fallback kernel).  In
 //           the BF16 wide units the thresholds are folded into the MMA: each
 //           query's -tau goes into three spare K columns of its operand row,
@@ -72,6 +73,22 @@ constexpr size_t LIST_BYTES = (size_t)LROW * BM * 4;
 constexpr int WARP_KEYS = 64;                     // sorted re-rank keys kept per epilogue warp
 constexpr int QROW4 = 16;                         // float4 of a staged query row (nC <= 64)
 constexpr int TAU_LOW_BIT = 12;                   // threshold search stops at this bit (2^-11 relative)
+// The threshold is the tau_rank-th smallest per-column minimum: tau_rank
+// distinct candidates lie at or below it, a margin over knn (<= 32) for the
+// rounding of the filter.  A list it cut must hold at least knn +
+// crowd_margin positive distances (exact copies of the query, at distance 0,
+// take places in it), else the query goes to the exact fallback.  BF16:
+// measured against FP64, rank 48 keeps the kNN recall at 1.0 with the same
+// rho / delta error as rank 64 on the 400k-spike drift site, a 1M-spike
+// sample of the probe batch and the test sites, with 20% less re-rank work;
+// rank 40 missed one neighbour on a 20k-spike site with exact duplicates (its
+// BF16 distance error, ~2^-8 |a| / d relative, crossed the gap between the
+// 30th and 40th neighbour), rank 44 did not.  FP8 (3 mantissa bits) keeps
+// rank 64.
+__host__ __device__ constexpr int tau_rank(bool fp8) { return fp8 ? 64 : 48; }
+__host__ __device__ constexpr int crowd_margin(bool fp8) { return fp8 ? 16 : 8; }
+static_assert(tau_rank(false) >= irc_tc::KNN_MAX + crowd_margin(false), "rank covers knn plus the margin");
+static_assert(tau_rank(true) >= irc_tc::KNN_MAX + crowd_margin(true), "rank covers knn plus the margin");
 static_assert((size_t)BROW * BM * 4 <= LIST_BYTES, "minima rows alias the list area");
 static_assert(LISTCAP <= irc_tc::LIST_MAX, "the re-rank takes every list the filter hands over");
 
@@ -182,7 +199,8 @@ template <int PER>
 __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL, bool complete, int q,
                                        const float *__restrict__ F, const float4 *__restrict__ Fp, int Dp4,
                                        float4 *__restrict__ qs, int nC, int knn, size_t o, unsigned long long *ws,
-                                       int lane, int *miKnn, float *d2Knn, float *vrKnn, float *rho, int *scratch)
+                                       int lane, int margin, int *miKnn, float *d2Knn, float *vrKnn, float *rho,
+                                       int *scratch)
 {
     const float *a = F + (size_t)q * nC;
     // the query row, staged once per warp (broadcast reads below)
@@ -219,7 +237,7 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
                 kv[bi] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
         }
     }
-    // A list cut by tau that holds fewer than knn + 16 positive distances
+    // A list cut by tau that holds fewer than knn + margin positive distances
     // (exact copies of the query, at distance 0 and excluded like the
     // reference's d > 0 test, crowded the threshold) may miss nearer
     // distinct candidates: such a query goes to the exact fallback.
@@ -227,7 +245,7 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
         unsigned nv = 0;
 #pragma unroll
         for (int i = 0; i < PER; ++i) nv += kv[i] != ~0ull;
-        if (__reduce_add_sync(0xffffffffu, nv) < (unsigned)(knn + 16)) {
+        if (__reduce_add_sync(0xffffffffu, nv) < (unsigned)(knn + margin)) {
             if (lane == 0) {
                 const int k = atomicAdd(scratch + 0, 1);
                 scratch[irc::kScratchLists + k] = q;
@@ -524,7 +542,8 @@ __device__ __forceinline__ void append_hits(uint32_t *lrow, int *cnt, unsigned m
 // (named barrier 1 + slot).
 template <int BN, bool TAU>
 __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::TcItem &it, const int (&nt)[4], int qps,
-                                         int bps, uint32_t tmem, uint8_t *sA, int tau_k, uint32_t *lists, float *sTau,
+                                         int bps, int rank, uint32_t tmem, uint8_t *sA, int tau_k, uint32_t *lists,
+                                         float *sTau,
                                          int *sCnt, uint64_t *acc_full, uint64_t *acc_empty, uint64_t *tau_ready,
                                          volatile int *abort_flag, const irc_tc::ListOut &lo, int *scratch, int warp,
                                          int lane)
@@ -580,7 +599,7 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
         __syncwarp();
         if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
     }
-    // threshold: 64th smallest of the 128 column minima of every query; the
+    // threshold: rank-th smallest of the 128 column minima of every query; the
     // minima rows of a quarter alias that quarter's own list rows
     float *qarea = reinterpret_cast<float *>(lists + (size_t)quarter * 32 * LROW);
     {
@@ -591,9 +610,9 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
         slot_barrier(s, slot_threads);
         // The warp's 8 rows at once (independent chains): a bitwise search,
         // from the top, of the largest t with fewer than 64 minima below it,
-        // i.e. of the 64th smallest minimum, on the non-negative float bit
+        // i.e. of the rank-th smallest minimum, on the non-negative float bit
         // patterns.  It stops at TAU_LOW_BIT and rounds up, so tau is an
-        // upper bound of the 64th smallest within 2^-11 of it (a few more
+        // upper bound of the rank-th smallest within 2^-11 of it (a few more
         // candidates listed, never fewer).
         constexpr int RL = 32 / PARTS;
         unsigned v4[RL][4], ans[RL];
@@ -611,7 +630,7 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
                 const unsigned t = ans[L] | (1u << b);
                 const unsigned c = (unsigned)(v4[L][0] < t) + (unsigned)(v4[L][1] < t) + (unsigned)(v4[L][2] < t) +
                                    (unsigned)(v4[L][3] < t);
-                if (__reduce_add_sync(0xffffffffu, c) < 64u) ans[L] = t;
+                if (__reduce_add_sync(0xffffffffu, c) < (unsigned)rank) ans[L] = t;
             }
         }
         if (lane < RL) {
@@ -904,7 +923,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
         }
         __syncwarp();
     } else {
-        epilogue<BN, TAU>(p, it, nt, qps, bps, tmem, sA, tau_k, lists, sTau, sCnt, acc_full, acc_empty, tau_ready, abort_flag,
+        epilogue<BN, TAU>(p, it, nt, qps, bps, tau_rank(FP8), tmem, sA, tau_k, lists, sTau, sCnt, acc_full, acc_empty, tau_ready, abort_flag,
                      lo, scratch, warp, lane);
     }
     sm100::tc_fence_before();
@@ -925,7 +944,7 @@ constexpr int RR_WARPS = 8;
 __global__ void __launch_bounds__(32 * RR_WARPS, 4)
 k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int n_out, int q_base,
          const float *__restrict__ F, const float4 *__restrict__ Fp, int nC, int knn, float *__restrict__ vrKnn,
-         float *__restrict__ rho, int *__restrict__ miKnn, float *__restrict__ d2Knn, int *__restrict__ scratch)
+         float *__restrict__ rho, int *__restrict__ miKnn, float *__restrict__ d2Knn, int margin, int *__restrict__ scratch)
 {
     __shared__ unsigned long long wkeys[RR_WARPS * WARP_KEYS];
     __shared__ float4 qrows[RR_WARPS * QROW4];
@@ -941,13 +960,13 @@ k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int
     unsigned long long *ws = wkeys + warp * WARP_KEYS;
     float4 *qs = qrows + warp * QROW4;
     if (cL <= 64)
-        rerank<2>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho,
+        rerank<2>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
                   scratch);
     else if (cL <= 128)
-        rerank<4>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho,
+        rerank<4>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
                   scratch);
     else
-        rerank<8>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, miKnn, d2Knn, vrKnn, rho,
+        rerank<8>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
                   scratch);
 }
 
@@ -1020,7 +1039,8 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
     if (rc != IRC_OK) return rc;
     if (ev) cudaEventRecord(ev[1], s);
     k_rerank<<<(n_out + RR_WARPS - 1) / RR_WARPS, 32 * RR_WARPS, 0, s>>>(
-        lo.qinfo, lo.lists, n_out, pl->dev.q_base, F, Fp, nC, knn, vrKnn, rho, miKnn, d2Knn, pl->scratch);
+        lo.qinfo, lo.lists, n_out, pl->dev.q_base, F, Fp, nC, knn, vrKnn, rho, miKnn, d2Knn, crowd_margin(fp8),
+        pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core) re-rank");
     if (ev) cudaEventRecord(ev[2], s);
     return IRC_OK;
