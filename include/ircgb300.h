@@ -106,6 +106,24 @@ int irc_delta_drift(float *vrDelta1, uint32_t *viNneigh1, const int32_t *miSite1
                     const float *mrFet2, const float *vrRho1, const int32_t *vnConst, float dc2,
                     void *stream);
 
+/* The distance cut-off of the time-drift clustering mode, calc_dc2_drift_
+ * (matlab/irc.m:24582-24608; cluster_drift_ computes it on its first drift
+ * window, :24095-24097, and passes it to every irc_rho_drift /
+ * irc_delta_drift call).  A window of n12 spikes, the own chunk's n1 first:
+ * viSite1 / viSite2 (HOST, [n12], 1-based primary / secondary sites, 0 =
+ * none), mrFet1 / mrFet2 (device, [nC x n12], primary / secondary features).
+ * Per site s = 1..nSites: up to dc_subsample own spikes on s (queries) and up
+ * to 4*dc_subsample window spikes with primary site s plus 4*dc_subsample with
+ * secondary site s (candidates), thinned by subsample_vr_; each query's
+ * squared distances (eucl2_dist_'s expansion form) sorted, entry
+ * ceil(n2 * dc_percent / 100) kept; the site's value is their median.  dc2
+ * (HOST) = the median over sites with queries (nanmedian); dc2_site (HOST,
+ * [nSites], may be NULL) = the per-site values, NaN for a site without
+ * queries.  dc_subsample <= 6400.  Synchronises the stream. */
+int irc_calc_dc2_drift(float *dc2, float *dc2_site, int n1, int n12, int nC, const int32_t *viSite1,
+                       const int32_t *viSite2, const float *mrFet1, const float *mrFet2, int nSites, int dc_subsample,
+                       double dc_percent, void *stream);
+
 /* The binned-minimum kNN variants of cuda_knn_index (same scan and selection
  * sort, so results depend on nThreads the same way).  vnConst (host) =
  * {nB, nA, nC, knn}; B: [nC x nB], A: [nC x nA]; knn <= nThreads.

@@ -36,6 +36,7 @@ SIGNATURES = {
     "irc_cuda_delta_knn": [_P, _P, _P, _P, _P, _P, _P, _I, _P],
     "irc_rho_drift": [_P, _P, _P, _P, _P, _F, _P],
     "irc_delta_drift": [_P, _P, _P, _P, _P, _P, _P, _F, _P],
+    "irc_calc_dc2_drift": [_P, _P, _I, _I, _I, _P, _P, _P, _P, _I, _I, C.c_double, _P],
     "irc_plan_create": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I],
     "irc_plan_destroy": [_P],
     "irc_plan_check": [_P, _P],

@@ -20,6 +20,10 @@ Reference call sites mirrored here:
   cuda_delta_knn_      matlab/irc.m:24519-24553  -> cuda_delta_knn_host
   cuda_rho_drift_      matlab/irc.m:24612-24637  -> cuda_rho_drift
   cuda_delta_drift_    matlab/irc.m:24641-24666  -> cuda_delta_drift
+  calc_dc2_drift_      matlab/irc.m:24582-24608  -> calc_dc2_drift
+  cluster_drift_       matlab/irc.m:24041-24180  -> cluster_drift (GPU branch)
+  rho_drift_knn_       matlab/irc.m:24336-24361  -> rho_drift_knn
+  delta_drift_knn_     matlab/irc.m:24477-24515  -> delta_drift_knn
   cuda_knn__           matlab/irc.m:24437-24465  -> knn_vr
   calc_drift_          matlab/irc2.m:6373-6465   -> calc_drift
   cuda_rho_, cuda_delta_ (time-window mode) matlab/irc.m:2528-2560, :2651-2688
@@ -497,6 +501,125 @@ def knn_vr(mrFet, vi2, vi1, knn=30, nThreads=256):
     vi2 = torch.as_tensor(vi2, device=mrFet.device, dtype=torch.long)
     vi1 = torch.as_tensor(vi1, device=mrFet.device, dtype=torch.long)
     return cuda_knn_kth(mrFet[vi2].contiguous(), mrFet[vi1].contiguous(), min(knn, vi2.numel()), nThreads)
+
+
+def calc_dc2_drift(n1, viSite1, viSite2, mrFet1, mrFet2, n_sites, dc_subsample=1000, dc_percent=2.0):
+    """calc_dc2_drift_ (matlab/irc.m:24582-24608) on the device
+    (irc_calc_dc2_drift): the distance cut-off of the time-drift mode for one
+    window (own chunk's n1 spikes first).  viSite1/viSite2: host int arrays of
+    1-based sites; mrFet1/mrFet2: device [n12, nC] primary / secondary
+    features.  Returns (dc2, dc2_site [n_sites], NaN where a site has no
+    queries)."""
+    s1, s2 = _i32host(viSite1), _i32host(viSite2)
+    f1, f2 = _dev_f32(mrFet1, mrFet1.device), _dev_f32(mrFet2, mrFet1.device)
+    dc2 = C.c_float()
+    site = np.zeros(n_sites, np.float32)
+    check(lib().irc_calc_dc2_drift(C.byref(dc2), site.ctypes.data_as(C.c_void_p), int(n1), int(f1.shape[0]),
+                                   int(f1.shape[1]), s1.ctypes.data_as(C.c_void_p), s2.ctypes.data_as(C.c_void_p),
+                                   _p(f1), _p(f2), int(n_sites), int(dc_subsample), float(dc_percent), _stream()),
+          "irc_calc_dc2_drift")
+    return np.float32(dc2.value), site
+
+
+def drift_windows(cviSpk_drift, miSort_drift):
+    """The drift windows of cluster_drift_ (matlab/irc.m:24084-24087): window
+    i = the spikes of chunks miSort_drift[:, i] (0-based chunk ids, its own
+    chunk first), concatenated; returns [(own spikes, window spikes)]."""
+    return [(np.asarray(own, np.int64),
+             np.concatenate([np.asarray(cviSpk_drift[j], np.int64) for j in miSort_drift[:, i]]))
+            for i, own in enumerate(cviSpk_drift)]
+
+
+def cluster_drift(viSite_spk, viSite2_spk, F1, F2, cviSpk_drift, miSort_drift, n_sites, dc_subsample=1000,
+                  dc_percent=2.0):
+    """rho, delta and nneigh of the time-drift mode (vcCluster = 'drift'):
+    the GPU branch of cluster_drift_ (matlab/irc.m:24041-24180).  dc2 comes
+    from the first window (calc_dc2_drift_); rho then delta window by window
+    (jrc3_cuda_rho_drift / jrc3_cuda_delta_drift, the window's own spikes
+    first); NaN deltas become the largest delta.  viSite_spk, viSite2_spk:
+    host 1-based sites of every spike; F1, F2: device [nSpk, nC] primary /
+    secondary features.  Returns dict(rho, delta, nneigh (0-based global),
+    dc2, dc2_site)."""
+    dev = F1.device
+    n = F1.shape[0]
+    rho = torch.zeros(n, dtype=torch.float32, device=dev)
+    delta = torch.zeros(n, dtype=torch.float32, device=dev)
+    nneigh = torch.zeros(n, dtype=torch.int64, device=dev)
+    s1_all, s2_all = np.asarray(viSite_spk, np.int32), np.asarray(viSite2_spk, np.int32)
+    wins = drift_windows(cviSpk_drift, miSort_drift)
+    dc2 = site = None
+    for own, w in wins:
+        wt = torch.as_tensor(w, device=dev)
+        f1, f2 = F1[wt].contiguous(), F2[wt].contiguous()
+        if dc2 is None:
+            dc2, site = calc_dc2_drift(len(own), s1_all[w], s2_all[w], f1, f2, n_sites, dc_subsample, dc_percent)
+        rho[torch.as_tensor(own, device=dev)] = cuda_rho_drift(s1_all[w], s2_all[w], f1, f2, len(own), dc2)
+    for own, w in wins:
+        wt = torch.as_tensor(w, device=dev)
+        d, nn = cuda_delta_drift(s1_all[w], s2_all[w], F1[wt].contiguous(), F2[wt].contiguous(), rho[wt],
+                                 len(own), dc2)
+        ot = torch.as_tensor(own, device=dev)
+        delta[ot] = d
+        nneigh[ot] = wt[nn.long() - 1]
+    bad = torch.isnan(delta)
+    if bad.any():
+        delta[bad] = delta[~bad].max()
+    return dict(rho=rho, delta=delta, nneigh=nneigh, dc2=dc2, dc2_site=site)
+
+
+def rho_drift_knn(mrFet12, viDrift_spk12, mlDrift, n1, knn=30, nC_max=45):
+    """rho_drift_knn_ (matlab/irc.m:24336-24361) for one site: for every drift
+    chunk, its own spikes (among the first n1) against the spikes of the
+    chunks linked to it (mlDrift[candidate chunk, chunk]) through cuda_knn_
+    (cuda_knn_index, knn = min(knn, n2)); rho = 1 ./ vrKnn; kNN lists shorter
+    than knn padded by repeating their last row.  viDrift_spk12: host 1-based
+    chunk ids of the n12 spikes; mlDrift: host bool [nT x nT].  Returns
+    (rho [n1], miKnn [n1, knn] 0-based into mrFet12)."""
+    vd = np.asarray(viDrift_spk12, np.int64)
+    ml = np.asarray(mlDrift, bool)
+    dev = mrFet12.device
+    rho = torch.zeros(n1, dtype=torch.float32, device=dev)
+    miKnn = torch.zeros((n1, knn), dtype=torch.long, device=dev)
+    for d in range(1, ml.shape[0] + 1):
+        vi1 = np.flatnonzero(vd[:n1] == d)
+        if not vi1.size:
+            continue
+        vi2 = np.flatnonzero(ml[vd - 1, d - 1])
+        K, I = cuda_knn(mrFet12, vi2, vi1, knn, nC_max)
+        t1 = torch.as_tensor(vi1, device=dev)
+        rho[t1] = 1.0 / K
+        if I.shape[1] < knn:
+            I = torch.cat([I, I[:, -1:].expand(-1, knn - I.shape[1])], 1)
+        miKnn[t1] = I
+    return rho, miKnn
+
+
+def delta_drift_knn(mrFet12, viDrift_spk12, mlDrift, vrRho12, n1):
+    """delta_drift_knn_ (matlab/irc.m:24477-24515) for one site: for every
+    drift chunk, cuda_delta_knn_ (cuda_delta_knn) of its own spikes against
+    the spikes of its linked chunks; delta .*= rho; a NaN or Inf delta becomes
+    sqrt(SINGLE_INF) with the spike's own position as nneigh.  Returns (delta
+    [n1], nneigh [n1] 0-based into mrFet12)."""
+    vd = np.asarray(viDrift_spk12, np.int64)
+    ml = np.asarray(mlDrift, bool)
+    dev = mrFet12.device
+    delta = torch.zeros(n1, dtype=torch.float32, device=dev)
+    nneigh = torch.zeros(n1, dtype=torch.long, device=dev)
+    for d in range(1, ml.shape[0] + 1):
+        vi1 = np.flatnonzero(vd[:n1] == d)
+        if not vi1.size:
+            continue
+        vi2 = np.flatnonzero(ml[vd - 1, d - 1])
+        D, N = cuda_delta_knn_host(mrFet12, vrRho12, vi2, vi1)
+        t1 = torch.as_tensor(vi1, device=dev)
+        delta[t1] = D
+        nneigh[t1] = N
+    delta = delta * vrRho12[:n1]
+    bad = ~torch.isfinite(delta)
+    pos = torch.arange(n1, device=dev)
+    nneigh = torch.where(bad, pos, nneigh)
+    delta = torch.where(bad, torch.full_like(delta, float(SQRT_SINGLE_INF_F)), delta)
+    return delta, nneigh
 
 
 def _dn_max(n1, n2, nTime_clu):

@@ -11,6 +11,8 @@
  *   [D, N] = ircgb300_mex('cuda_delta_knn',     B, A, R_B, R_A, vnConst, nThreads)
  *   rho    = ircgb300_mex('rho_drift',          miSite12, mrFet1, mrFet2, vnConst, dc2)
  *   [D, N] = ircgb300_mex('delta_drift',        miSite12, mrFet1, mrFet2, vrRho1, vnConst, dc2)
+ *   [dc2, vrDc2_site] = ircgb300_mex('calc_dc2_drift', n1, viSite1, viSite2, mrFet1, mrFet2, nSites,
+ *                                    dc_subsample, dc_percent)
  *   K      = ircgb300_mex('cuda_knn',           B, A, vnConst, nThreads)
  *   [K, I] = ircgb300_mex('cuda_knn_full',      B, A, vnConst, nThreads)
  *   [K, I] = ircgb300_mex('cuda_knn_ib',        B, A, IB, vnConst, nThreads)
@@ -190,6 +192,33 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         if (nlhs > 1) plhs[1] = mxGPUCreateMxArrayOnGPU(N);
         mxGPUDestroyGPUArray(D); mxGPUDestroyGPUArray(N);
         mxGPUDestroyGPUArray(S); mxGPUDestroyGPUArray(F1); mxGPUDestroyGPUArray(F2); mxGPUDestroyGPUArray(R);
+        return;
+    }
+    if (!strcmp(cmd, "calc_dc2_drift")) {
+        const int n1 = (int)mxGetScalar(prhs[1]), n12 = (int)mxGetNumberOfElements(prhs[2]);
+        const int nSites = (int)mxGetScalar(prhs[6]);
+        const mxGPUArray *F1 = gin(prhs[4]), *F2 = gin(prhs[5]);
+        int32_t *s1 = (int32_t *)mxMalloc(sizeof(int32_t) * (size_t)(n12 > 0 ? n12 : 1));
+        int32_t *s2 = (int32_t *)mxMalloc(sizeof(int32_t) * (size_t)(n12 > 0 ? n12 : 1));
+        host_i32(prhs[2], s1, n12);
+        host_i32(prhs[3], s2, n12);
+        float dc2 = 0.0f;
+        float *site = (float *)mxCalloc((size_t)(nSites > 0 ? nSites : 1), sizeof(float));
+        const int nC = n12 > 0 ? (int)(mxGPUGetNumberOfElements(F1) / (size_t)n12) : 0;
+        rc = irc_calc_dc2_drift(&dc2, site, n1, n12, nC, s1, s2, (const float *)mxGPUGetDataReadOnly(F1),
+                                (const float *)mxGPUGetDataReadOnly(F2), nSites, (int)mxGetScalar(prhs[7]),
+                                mxGetScalar(prhs[8]), NULL);
+        mxFree(s1);
+        mxFree(s2);
+        mxGPUDestroyGPUArray(F1);
+        mxGPUDestroyGPUArray(F2);
+        if (rc != IRC_OK) { mxFree(site); fail(rc, cmd); }
+        plhs[0] = mxCreateDoubleScalar((double)dc2);
+        if (nlhs > 1) {
+            plhs[1] = mxCreateNumericMatrix((mwSize)nSites, 1, mxSINGLE_CLASS, mxREAL);
+            memcpy(mxGetData(plhs[1]), site, sizeof(float) * (size_t)nSites);
+        }
+        mxFree(site);
         return;
     }
     if (!strcmp(cmd, "cuda_knn") || !strcmp(cmd, "cuda_knn_full") || !strcmp(cmd, "cuda_knn_ib")) {

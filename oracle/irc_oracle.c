@@ -873,3 +873,132 @@ void orc_delta_drift(float *vrDelta1, uint32_t *viNneigh1, const int32_t *miSite
         viNneigh1[i1] = bi + 1;
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* 3d. calc_dc2_drift_ (matlab/irc.m:24582-24608)                            */
+/* ------------------------------------------------------------------------ */
+
+/* subsample_vr_ (matlab/irc.m:11322-11337) on a list of n 0-based positions,
+ * in place; returns the new length.  Every nSkip-th entry (nSkip =
+ * floor(n / nMax) when above 1), then the entries at round(linspace(1, n',
+ * nRemove)) removed, MATLAB's linspace being d1 + ((0:m-1) (d2 - d1)) / (m-1)
+ * with its first and last points set to d1 and d2 (a one-point linspace is
+ * d2), MATLAB's round half away from zero. */
+static int dc2_subsample(int32_t *vi, int n, int nMax)
+{
+    if (n <= nMax) return n;
+    const int nSkip = n / nMax;
+    if (nSkip > 1) {
+        int m = 0;
+        for (int i = 0; i < n; i += nSkip) vi[m++] = vi[i];
+        n = m;
+    }
+    if (n > nMax) {
+        const int nRemove = n - nMax;
+        char *rm = (char *)calloc((size_t)n, 1);
+        for (int i = 0; i < nRemove; ++i) {
+            double y;
+            if (nRemove == 1) y = n;
+            else if (i == 0) y = 1.0;
+            else if (i == nRemove - 1) y = n;
+            else y = 1.0 + ((double)i * ((double)n - 1.0)) / (double)(nRemove - 1);
+            long r = lround(y);
+            if (r < 1) r = 1;
+            if (r > n) r = n;
+            rm[r - 1] = 1;
+        }
+        int m = 0;
+        for (int i = 0; i < n; ++i)
+            if (!rm[i]) vi[m++] = vi[i];
+        free(rm);
+        n = m;
+    }
+    return n;
+}
+
+static int cmp_float_nan_last(const void *pa, const void *pb)
+{
+    const float a = *(const float *)pa, b = *(const float *)pb;
+    const int na = a != a, nb = b != b;
+    if (na || nb) return na - nb;
+    return (a > b) - (a < b);
+}
+
+/* MATLAB median of single values: NaN if any (or none); the middle value, or
+ * a + (b - a) / 2 of the two middle values ((a + b) / 2 when their signs
+ * differ or one is infinite). */
+static float dc2_median(float *v, int n)
+{
+    if (n == 0) return NAN;
+    for (int i = 0; i < n; ++i)
+        if (v[i] != v[i]) return NAN;
+    qsort(v, (size_t)n, sizeof(float), cmp_float_nan_last);
+    if (n & 1) return v[n / 2];
+    const float a = v[n / 2 - 1], b = v[n / 2];
+    if (signbit(a) != signbit(b) || isinf(a) || isinf(b)) return (a + b) / 2.0f;
+    return a + (b - a) / 2.0f;
+}
+
+/* calc_dc2_drift_: window of n12 spikes (its own chunk's n1 first), sites
+ * 1-based (viSite1 primary, viSite2 secondary), features F1 / F2 [n12 x nC]
+ * (primary / secondary, MATLAB [nC x n12]).  Per site: queries = subsample of
+ * the own spikes on the site (dc_subsample), candidates = subsample of the
+ * window spikes with that primary site (4 dc_subsample, F1) then of those with
+ * that secondary site (4 dc_subsample, F2); squared distances in eucl2_dist_'s
+ * expansion form yy + (xx - 2 xy) (yy, xx: rounded squares summed in feature
+ * order; xy: fused multiply-adds in feature order), each query's sorted
+ * distances cut at entry ceil(n2 * dc_percent / 100); site dc2 = median over
+ * its queries.  Returns the nanmedian over sites; dc2_site [nSites] (NULL
+ * allowed) receives the per-site values (NaN for a site without queries). */
+float orc_calc_dc2_drift(float *dc2_site, int n1, int n12, int nC, const int32_t *viSite1, const int32_t *viSite2,
+                         const float *F1, const float *F2, int nSites, int dc_subsample, double dc_percent)
+{
+    int32_t *v11 = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n12 + 1));
+    int32_t *v21 = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n12 + 1));
+    int32_t *v22 = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n12 + 1));
+    float *sites = (float *)malloc(sizeof(float) * (size_t)nSites);
+    int ns = 0;
+    for (int s = 0; s < nSites; ++s) {
+        const int site = s + 1;
+        int a = 0, b = 0, c = 0;
+        for (int i = 0; i < n12; ++i) {
+            if (i < n1 && viSite1[i] == site) v11[a++] = i;
+            if (viSite1[i] == site) v21[b++] = i;
+            if (viSite2[i] == site) v22[c++] = i;
+        }
+        a = dc2_subsample(v11, a, dc_subsample);
+        b = dc2_subsample(v21, b, 4 * dc_subsample);
+        c = dc2_subsample(v22, c, 4 * dc_subsample);
+        const int n2 = b + c;
+        float m = NAN;
+        if (a > 0 && n2 > 0) {
+            const int icut = (int)ceil((double)n2 * dc_percent / 100.0);
+            float *d = (float *)malloc(sizeof(float) * (size_t)n2);
+            float *cut = (float *)malloc(sizeof(float) * (size_t)a);
+            for (int q = 0; q < a; ++q) {
+                const float *y = F1 + (size_t)v11[q] * nC;
+                float yy = 0.0f;
+                for (int k = 0; k < nC; ++k) yy = yy + y[k] * y[k];
+                for (int j = 0; j < n2; ++j) {
+                    const float *x = j < b ? F1 + (size_t)v21[j] * nC : F2 + (size_t)v22[j - b] * nC;
+                    float xx = 0.0f, xy = 0.0f;
+                    for (int k = 0; k < nC; ++k) {
+                        xx = xx + x[k] * x[k];
+                        xy = fmaf(x[k], y[k], xy);
+                    }
+                    d[j] = yy + (xx - 2.0f * xy);
+                }
+                qsort(d, (size_t)n2, sizeof(float), cmp_float_nan_last);
+                cut[q] = d[icut - 1];
+            }
+            m = dc2_median(cut, a);
+            free(d);
+            free(cut);
+        }
+        if (dc2_site) dc2_site[s] = m;
+        if (m == m) sites[ns++] = m;
+    }
+    const float r = dc2_median(sites, ns);
+    free(v11); free(v21); free(v22); free(sites);
+    return r;
+}

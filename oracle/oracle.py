@@ -11,6 +11,8 @@ calls it.
 * ``exact_knn_f64`` / ``exact_delta_f64``: double-precision ground truth.
 * ``site_knn_cpu`` / ``site_delta_cpu``: the reference CPU path (knn_cpu_,
   delta_cpu_), also the timed CPU baseline.
+* ``calc_dc2_drift``: the distance cut-off of the time-drift clustering mode
+  (calc_dc2_drift_, matlab/irc.m:24582-24608).
 * ``sort_rho`` / ``assign_cluster_knn``: the clustering step after the
   path -- sort_'s rho normalisation and ordrho (matlab/irc2.m:3263-3264),
   postCluster_ / assignCluster_knn_ / cell2map_ / dpclus_remove_count_
@@ -48,6 +50,9 @@ def lib():
                      "orc_cuda_knn_full", "orc_cuda_knn_ib", "orc_cuda_rho", "orc_cuda_delta"):
             getattr(_lib, name).restype = None
         _lib.orc_assign_cluster_knn.restype = C.c_int
+        _lib.orc_calc_dc2_drift.restype = C.c_float
+        _lib.orc_calc_dc2_drift.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, C.c_int, C.c_int,
+                                            C.c_double]
     return _lib
 
 
@@ -282,6 +287,18 @@ def site_delta_cpu(F, R, plan):
                              _ptr(q0), _ptr(nq), _ptr(roff), _ptr(rs), _ptr(rn),
                              C.c_int(len(q0)), C.c_int(qb))
     return de, nn
+
+
+def calc_dc2_drift(n1, viSite1, viSite2, F1, F2, n_sites, dc_subsample=1000, dc_percent=2.0):
+    """calc_dc2_drift_ (matlab/irc.m:24582-24608) restated: (dc2, dc2_site).
+    viSite1/viSite2: 1-based sites of the window's n12 spikes (own chunk's n1
+    first); F1/F2: primary / secondary features [n12, nC]."""
+    F1, F2 = _fet(F1), _fet(F2)
+    s1, s2 = _i32(viSite1), _i32(viSite2)
+    site = np.zeros(n_sites, np.float32)
+    d = lib().orc_calc_dc2_drift(_ptr(site), int(n1), int(F1.shape[0]), int(F1.shape[1]), _ptr(s1), _ptr(s2),
+                                 _ptr(F1), _ptr(F2), int(n_sites), int(dc_subsample), float(dc_percent))
+    return np.float32(d), site
 
 
 # --- clustering after the path ---------------------------------------------------------

@@ -28,6 +28,7 @@ int mxGetString(const mxArray *a, char *buf, mwSize n);
 void mxSetM(mxArray *a, mwSize m);
 void mxSetN(mxArray *a, mwSize n);
 mxArray *mxCreateDoubleScalar(double v);
+mxArray *mxCreateNumericMatrix(mwSize m, mwSize n, mxClassID cls, mxComplexity c);
 void mxDestroyArray(mxArray *a);
 void *mxMalloc(mwSize n);
 void *mxCalloc(mwSize n, mwSize size);
