@@ -211,6 +211,15 @@ int irc_plan_tc_layout(irc_plan *plan, int max_slots, int order);
 size_t irc_plan_tc_bytes(const irc_plan *plan, int nC);
 int irc_plan_set_tc_buffer(irc_plan *plan, void *buf, size_t bytes);
 
+/* Poll limit of the tensor-core filter's pipeline waits on the current
+ * device: polls > 0 sets it, polls <= 0 restores the default (~2^22 polls
+ * with back-off, a few seconds).  A wait that runs out makes its CTA stop,
+ * let its own copies and MMAs land, free its TMEM and set the plan's error
+ * word, which irc_plan_check reports as IRC_E_TIMEOUT; a small limit
+ * exercises that path.  Applies to later calls; not during stream capture.
+ * No reference counterpart (the reference kernels have no waits). */
+int irc_set_wait_limit(int polls);
+
 /* Kernel timing of the tensor-core modes.  Between irc_profile_begin and
  * irc_profile_end every tensor-core irc_site_knn call (up to max_calls)
  * records CUDA events on its stream around its filter kernel and around its

@@ -47,6 +47,7 @@ SIGNATURES = {
     "irc_batch_plan_create": [_P, _I, _P, _P, _P, _P, _P, _P, _P],
     "irc_batch_stack": [_P, _I, _P, _P, _P, _I, _P],
     "irc_profile_begin": [_I],
+    "irc_set_wait_limit": [_I],
     "irc_profile_end": [_P, _P, _P],
     "irc_site_knn": [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P],
     "irc_site_delta": [_P, _P, _I, _P, _I, _I, _I, _P, _P, _P, _P, _P],

@@ -63,20 +63,36 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity)
 }
 
 // Bounded wait for the phase with the given parity: a few non-blocking
-// probes, then try_wait with back-off.  On timeout the shared error word is
-// set and false returned; callers then stop their pipeline.  The limit
-// (~2^22 polls with back-off, a few seconds) is far above any legitimate
-// wait of these kernels.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag)
+// probes, then try_wait with back-off, at most `limit` polls in all.  On
+// timeout the shared abort word is set and false returned; a wait that finds
+// the word set gives up too, so every role of the CTA stops its pipeline.
+// The default limit (~2^22 polls with back-off, a few seconds) is far above
+// any legitimate wait of these kernels.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                          uint32_t limit = (1u << 22))
 {
-    for (int f = 0; f < 64; ++f)
+    const uint32_t probes = limit < 64u ? limit : 64u;
+    for (uint32_t f = 0; f < probes; ++f)
         if (mbar_test_wait(bar, parity)) return true;
-    for (uint32_t i = 0; i < (1u << 22); ++i) {
+    for (uint32_t i = probes; i < limit; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
         if (i > 32) __nanosleep(i > 4096 ? 256 : 32);
     }
     *abort_flag = 1;
+    return false;
+}
+
+// Wait for a phase that an operation this CTA issued completes (its own TMA
+// loads, its MMAs), whatever the abort word: a CTA that gave up still lets
+// them land before it frees TMEM or exits.  Bounded (~2^22 polls with
+// back-off); false only if even that runs out.
+__device__ __forceinline__ bool mbar_drain(uint64_t *bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < (1u << 22); ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (i > 32) __nanosleep(i > 4096 ? 256 : 32);
+    }
     return false;
 }
 
@@ -140,24 +156,6 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
-}
-
-// 32 consecutive f32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
-{
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // 16 consecutive f32 columns of this thread's TMEM lane, without the wait:

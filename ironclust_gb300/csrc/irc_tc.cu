@@ -55,6 +55,10 @@
 #include "irc_sm100.cuh"
 #include "irc_tc.cuh"
 
+// Poll limit of the filter's pipeline waits (irc_set_wait_limit); the
+// drains of a CTA's own copies and MMAs keep the full bound.
+__constant__ uint32_t c_wait_polls = 1u << 22;
+
 namespace {
 
 using irc_tc::BM;
@@ -119,6 +123,13 @@ template <int BN>
 __device__ __forceinline__ int units_per_pass(int nts)
 {
     return BN == 256 ? (nts + 1) >> 1 : nts;
+}
+
+// A wait of the filter's pipeline (see sm100::mbar_wait), bounded by the
+// poll limit set with irc_set_wait_limit.
+__device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag)
+{
+    return sm100::mbar_wait(bar, parity, abort_flag, c_wait_polls);
 }
 
 // Ascending bitonic sort of 32*PER keys held PER per lane (element e = lane*PER + i).
@@ -585,7 +596,7 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
         int ra, na, rb, nb;
         unit(k, ra, na, rb, nb);
         const int b = s * bps + (k & (bps - 1));
-        if (!(ok = sm100::mbar_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
+        if (!(ok = pipe_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
         sm100::tc_fence_after();
         if (active) {
             if constexpr (BN == 256) {
@@ -658,7 +669,7 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
         int ra, na, rb, nb;
         unit(k, ra, na, rb, nb);
         const int b = s * bps + (k & (bps - 1));
-        if (!(ok = sm100::mbar_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
+        if (!(ok = pipe_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
         sm100::tc_fence_after();
         if (active && (na > 0 || nb > 0)) {
             unsigned ma = 0u, mb = 0u;
@@ -757,7 +768,7 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
                 any = true;
                 const int u = k % U[s];
                 const int st = i % T::STAGES;
-                if ((ok = sm100::mbar_wait(&empty[st], ((i / T::STAGES) & 1) ^ 1, abort_flag))) {
+                if ((ok = pipe_wait(&empty[st], ((i / T::STAGES) & 1) ^ 1, abort_flag))) {
                     uint8_t *dst = sB + (size_t)st * T::STAGE_BYTES;
                     const int nh = BN == 256 && 2 * u + 1 < nt[s] ? 2 : 1;   // 128-tiles of the unit
                     sm100::mbar_arrive_expect_tx(&full[st], nh * HALF_BYTES);
@@ -774,8 +785,8 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
     }
     // every issued load has landed before the CTA exits
     for (int j = (i > T::STAGES ? i - T::STAGES : 0); j < i; ++j)
-        sm100::mbar_wait(&full[j % T::STAGES], (j / T::STAGES) & 1, abort_flag);
-    sm100::mbar_wait(a_full, 0, abort_flag);
+        sm100::mbar_drain(&full[j % T::STAGES], (j / T::STAGES) & 1);
+    sm100::mbar_drain(a_full, 0);
 }
 
 // MMA issuer (one thread), in the producer's order; slot s's unit k goes to
@@ -794,7 +805,7 @@ __device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem,
     // bf16 x bf16 (kind::f16, K = 16) or e4m3 x e4m3 (kind::f8f6f4, K = 32) -> f32;
     // either way one MMA consumes 32 bytes of every 128-byte operand row
     constexpr uint32_t idesc = FP8 ? sm100::idesc_make(BM, BN, 0, 0) : sm100::idesc_make(BM, BN, 1, 1);
-    if (sm100::mbar_wait(a_full, 0, abort_flag)) {
+    if (pipe_wait(a_full, 0, abort_flag)) {
         sm100::tc_fence_after();
         const uint64_t adesc = sm100::sdesc_sw128(sm100::smem_u32(sA));
         int U[NS];
@@ -809,10 +820,10 @@ __device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem,
                 if (ok && k < 2 * U[s]) {
                     any = true;
                     const int b = s * BPS + k % BPS, st = i % T::STAGES;
-                    ok = (k < BPS || sm100::mbar_wait(&acc_empty[b], ((k - BPS) / BPS) & 1, abort_flag)) &&
-                         sm100::mbar_wait(&full[st], (i / T::STAGES) & 1, abort_flag) &&
+                    ok = (k < BPS || pipe_wait(&acc_empty[b], ((k - BPS) / BPS) & 1, abort_flag)) &&
+                         pipe_wait(&full[st], (i / T::STAGES) & 1, abort_flag) &&
                          // the slot's thresholds are in the query tile before its pass 2
-                         (!TAU || k != U[s] || sm100::mbar_wait(&tau_ready[s], 0, abort_flag));
+                         (!TAU || k != U[s] || pipe_wait(&tau_ready[s], 0, abort_flag));
                     if (ok) {
                         sm100::tc_fence_after();
                         const uint64_t bdesc =
@@ -836,7 +847,7 @@ __device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem,
     }
     // every MMA has completed before TMEM is released
     sm100::mma_commit(mma_done);
-    sm100::mbar_wait(mma_done, 0, abort_flag);
+    sm100::mbar_drain(mma_done, 0);
 }
 
 // The filter over the work items of one unit width (items of one or two slots
@@ -1049,6 +1060,14 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
 }  // namespace irc_tc
 
 extern "C" {
+
+int irc_set_wait_limit(int polls)
+{
+    const uint32_t v = polls > 0 ? (uint32_t)polls : (1u << 22);
+    cudaError_t e = cudaMemcpyToSymbol(c_wait_polls, &v, sizeof(v));
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_set_wait_limit");
+    return IRC_OK;
+}
 
 int irc_profile_begin(int max_calls)
 {
