@@ -23,18 +23,31 @@ class SiteBatch:
 
     def __init__(self, sites):
         sites = list(sites)
-        self.n_sites = len(sites)
-        self.dims = np.array([s["F"].shape[1] for s in sites], np.int32)
-        self.sizes = np.array([s["F"].shape[0] for s in sites], np.int64)
+        Fs = [s["F"] for s in sites]
+        plans = [build_plan(s["viDrift"], np.ones(s["F"].shape[0], bool), s["mlDrift"]) for s in sites]
+        self._stack(Fs, plans)
+
+    def subset(self, idx):
+        """The batch of sites idx (in that order), e.g. one rank's share.  It
+        keeps this batch's padded width, so every kernel sees the same
+        feature layout and its results equal this batch's rows bit for bit."""
+        out = SiteBatch.__new__(SiteBatch)
+        out._stack([self.F[self.site_slice(i), :int(self.dims[i])] for i in idx], [self.site_plans[i] for i in idx],
+                   width=self.F.shape[1])
+        return out
+
+    def _stack(self, Fs, plans, width=None):
+        self.n_sites = len(Fs)
+        self.dims = np.array([f.shape[1] for f in Fs], np.int32)
+        self.sizes = np.array([f.shape[0] for f in Fs], np.int64)
         self.bases = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
-        n, dmax = int(self.bases[-1]), int(self.dims.max())
+        n, dmax = int(self.bases[-1]), int(width or self.dims.max())
         self.F = np.zeros((n, dmax), np.float32)
         q0, nq, rs, rn, roff, site_of_chunk = [], [], [], [], [0], []
         self.site_plans = []
-        for i, s in enumerate(sites):
+        for i, (f, p) in enumerate(zip(Fs, plans)):
             b = int(self.bases[i])
-            self.F[b:b + s["F"].shape[0], :s["F"].shape[1]] = s["F"]
-            p = build_plan(s["viDrift"], np.ones(s["F"].shape[0], bool), s["mlDrift"])
+            self.F[b:b + f.shape[0], :f.shape[1]] = f
             self.site_plans.append(p)
             q0.append(p["q0"] + b)
             nq.append(p["nq"])
@@ -79,7 +92,7 @@ class SiteBatch:
 
         from ._lib import check, lib
         dev = F_sites[0].device
-        n, dmax = int(self.bases[-1]), int(self.dims.max())
+        n, dmax = int(self.bases[-1]), int(self.F.shape[1])
         out = torch.empty((n, dmax), dtype=torch.float32, device=dev)
         ptrs = (C.c_void_p * self.n_sites)(*[t.data_ptr() for t in F_sites])
         nc = np.ascontiguousarray(self.dims, np.int32)

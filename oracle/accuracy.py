@@ -106,3 +106,59 @@ def compare(out, ref, queries=None):
                    nneigh_rho_order_flips=int(flip.sum()), nneigh_errors=int(err.sum()),
                    delta_above_1e4=int((drel[ok_d] > 1e-4).sum()))
     return res
+
+
+def stream_block_check(st, k, knn):
+    """Accuracy of block k of a streamed pass (st: a stream.Streamer after
+    run()) against FP64: kNN recall, rho and delta with the same rules as
+    compare().  Block k's candidates and higher-rho neighbours lie in blocks
+    k-1 .. k+1, so the FP64 kNN runs on those three blocks (their rho64), the
+    FP64 delta on block k; everything is checked in the coordinates of that
+    three-block window of the recording."""
+    wl = st.wl
+    nb, base, D = wl["n_blocks"], wl["block_base"], wl["n_dim"]
+    ring = np.zeros((st.N_SLOTS * st.slot_rows, D), np.float32)
+    for j in range(k - 2, k + 3):                # blocks k-1 .. k+1 read their own neighbours
+        if 0 <= j < nb:
+            a, z = int(base[j]), int(base[j + 1])
+            ring[st._slot(j):st._slot(j) + (z - a)] = wl["F16"][a:z].numpy()
+    js = [j for j in (k - 1, k, k + 1) if 0 <= j < nb]
+    lo, hi = int(base[js[0]]), int(base[js[-1] + 1])
+    W = hi - lo
+
+    def to_window(ids):                          # 1-based ring rows of block k's plan -> window rows
+        ids = np.asarray(ids, np.int64)
+        out = np.zeros_like(ids)
+        for j in js:
+            r0, n = st._slot(j), int(base[j + 1] - base[j])
+            sel = (ids > r0) & (ids <= r0 + n)
+            out[sel] = ids[sel] - r0 + (int(base[j]) - lo)
+        return out
+
+    R = np.full(ring.shape[0], -np.inf)
+    ref = dict(idx=np.zeros((W, knn), np.int64), d2=np.full((W, knn), np.nan), rho=np.full(W, np.nan),
+               nneigh=np.zeros(W, np.int64), delta=np.full(W, np.inf))
+    for j in js:
+        idx, d2 = O.exact_knn_f64(ring, dict(st.plans[j].d), knn)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            rho = 1.0 / np.sqrt(d2[:, knn - 1])
+        n, w0 = int(base[j + 1] - base[j]), int(base[j]) - lo
+        R[st._slot(j):st._slot(j) + n] = np.where(np.isnan(rho), -np.inf, rho)
+        ref["rho"][w0:w0 + n] = rho
+        if j == k:
+            ref["idx"][w0:w0 + n] = to_window(idx)
+            ref["d2"][w0:w0 + n] = d2
+    nn, dd = O.exact_delta_f64(ring, R, dict(st.plans[k].d))
+    a, z = int(base[k]), int(base[k + 1])
+    q = np.arange(a - lo, z - lo)
+    ref["nneigh"][q] = to_window(nn)
+    with np.errstate(invalid="ignore"):
+        ref["delta"][q] = np.sqrt(dd) * ref["rho"][q]
+    out = dict(rho=st.out["rho"][lo:hi].numpy(), miKnn=np.zeros((W, knn), np.int64),
+               nneigh=np.zeros(W, np.int64), delta=np.zeros(W, np.float32))
+    out["miKnn"][q] = to_window(st.out["miKnn"][a:z].numpy())
+    out["nneigh"][q] = to_window(st.out["nneigh"][a:z].numpy())
+    out["delta"][q] = st.out["delta"][a:z].numpy()
+    res = compare(out, ref, q)
+    res.update(block=int(k), block_spikes=int(z - a))
+    return res

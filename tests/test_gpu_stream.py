@@ -1,13 +1,13 @@
 """The page-streaming pipeline (FP16 host features, a five-block device ring,
 overlapped copies, kNN one block ahead of delta) gives the results of the
-same block plans run directly, and the BF16 form keeps its recall and rho
-accuracy against the FP64 oracle."""
+same block plans run directly, and the BF16 form keeps its recall, rho and
+delta accuracy against the FP64 oracle."""
 import numpy as np
 import pytest
 import torch
 
 from ironclust_gb300 import irc, stream
-from oracle import oracle as O
+from oracle import accuracy as A
 
 pytestmark = pytest.mark.gpu
 
@@ -56,21 +56,20 @@ def test_stream_matches_direct_plans(streamed, k):
     assert np.array_equal(st.out["nneigh"][a:z].numpy(), nneigh.cpu().numpy())
 
 
-def test_stream_recall_vs_fp64(streamed):
+@pytest.mark.parametrize("where", ["first", "middle", "last"])
+def test_stream_accuracy_vs_fp64(streamed, where):
+    """kNN recall, rho and delta (nearest higher-rho neighbour included) of a
+    streamed block against FP64 (oracle.accuracy.stream_block_check: FP64
+    kNN on the block and its two neighbours, FP64 delta on the block)."""
     wl, st, _ = streamed
-    k = wl["n_blocks"] // 2
-    F = st.ring_rows(k)
-    plan = dict(st.plans[k].d)
-    i64, d64 = O.exact_knn_f64(F, plan, 30)
-    a, z = st.block_rows(k)
-    got = st.out["miKnn"][a:z].numpy()
-    nval = np.isfinite(d64).sum(1)
-    hits = sum(len(set(x[:v]) & set(y[:v])) for x, y, v in zip(got, i64, nval))
-    assert hits / nval.sum() >= 0.999
-    ok = np.isfinite(d64[:, 29])
-    rho64 = 1.0 / np.sqrt(d64[ok, 29])
-    rel = np.abs(st.out["rho"][a:z].numpy()[ok] - rho64) / rho64
-    assert rel.max() <= 1e-4, rel.max()
+    k = {"first": 0, "middle": wl["n_blocks"] // 2, "last": wl["n_blocks"] - 1}[where]
+    acc = A.stream_block_check(st, k, 30)
+    assert acc["checked"] == acc["block_spikes"] > 0
+    assert acc["recall_vs_fp64"] >= 0.999, acc
+    assert acc["rho_max_rel_err"] <= 1e-5, acc
+    assert acc["delta_checked"] > 0.9 * acc["checked"], acc
+    assert acc["delta_max_rel_err"] <= 1e-5, acc
+    assert acc["nneigh_errors"] == 0, acc
 
 
 def test_stream_global_rows(streamed):
