@@ -650,6 +650,8 @@ extern "C" int irc_site_knn_exact_noalloc(const float *F, int nC, const int32_t 
     p.roffr = d_roff; p.rsr = d_rs; p.rnr = d_rn;         // the EXACT kernels take any run split
     for (int k = 0; k < irc::kNumTileSizes; ++k) p.tile_off[k] = d_tile;     // only the 16-query table is read
     p.ncand = nullptr;                                    // read only by the delta kernels
+    p.tc_toff = nullptr;                                  // read only by the tensor-core filter
+    p.tc_tiles = nullptr;
     p.nChunks = nChunks; p.q_base = q_base; p.n_out = n_out; p.nF = nF; p.nRuns = nRuns;
     const size_t smem = (size_t)kQB * kCap * 8 + (size_t)kQB * kThreads * 4;
     e = cudaFuncSetAttribute(k_site_knn_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -41,6 +41,12 @@ struct PlanDev {
     const int32_t *roffr, *rsr, *rnr;
     const int32_t *tile_off[kNumTileSizes];   // [nChunks+1] prefix sums of ceil(nq/QB)
     const int32_t *ncand;                     // [nChunks] candidates of each chunk (sum of its runs)
+    // 128-candidate tiles of every chunk's intervals for the tensor-core
+    // filter: tile j of chunk c is tc_tiles[tc_toff[c] + j] = (first row,
+    // columns); each chunk's list is padded to an even length with (0, 0),
+    // so a 256-wide unit is one aligned int4.  Null in plans without it.
+    const int32_t *tc_toff;                   // [nChunks+1]
+    const int2 *tc_tiles;
     int nChunks, q_base, n_out, nF, nRuns;
 };
 

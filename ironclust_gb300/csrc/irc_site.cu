@@ -424,6 +424,23 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
         for (int r = roff[i]; r < roff[i + 1]; ++r) c += rn[r];
         img.push_back(c);
     }
+    // tensor-core tiles: every chunk's intervals cut into 128-row tiles,
+    // each chunk's list padded to an even length
+    const size_t off_toff = img.size();
+    std::vector<int32_t> tiles;
+    for (int i = 0; i < nChunks; ++i) {
+        img.push_back((int32_t)(tiles.size() / 2));
+        for (int r = moff[i]; r < moff[i + 1]; ++r)
+            for (int t = 0; t < mn[r]; t += 128) {
+                tiles.push_back(ms[r] + t);
+                tiles.push_back(std::min(128, mn[r] - t));
+            }
+        if ((tiles.size() / 2) & 1) { tiles.push_back(0); tiles.push_back(0); }
+    }
+    img.push_back((int32_t)(tiles.size() / 2));
+    while (img.size() % 4) img.push_back(0);          // 16-byte aligned
+    const size_t off_tiles = img.size();
+    img.insert(img.end(), tiles.begin(), tiles.end());
     size_t off_tile[irc::kNumTileSizes];
     for (int k = 0; k < irc::kNumTileSizes; ++k) {
         const int qb = irc::kTileSizes[k];
@@ -471,6 +488,8 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     pl->dev.rsr = base + off_rsr;
     pl->dev.rnr = base + off_rnr;
     pl->dev.ncand = base + off_ncand;
+    pl->dev.tc_toff = base + off_toff;
+    pl->dev.tc_tiles = reinterpret_cast<const int2 *>(base + off_tiles);
     for (int k = 0; k < irc::kNumTileSizes; ++k) pl->dev.tile_off[k] = base + off_tile[k];
     pl->scratch = (int32_t *)pl->dmem + img.size();
     pl->tc_items = reinterpret_cast<const irc::TcItem *>((const int32_t *)pl->dmem + off_items);

@@ -62,22 +62,25 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity: a few non-blocking
-// probes, then try_wait with back-off, at most `limit` polls in all.  On
-// timeout the shared abort word is set and false returned; a wait that finds
-// the word set gives up too, so every role of the CTA stops its pipeline.
-// The default limit (~2^22 polls with back-off, a few seconds) is far above
-// any legitimate wait of these kernels.
+// Bounded wait for the phase with the given parity: up to `probes`
+// non-blocking tests (cheap when the phase has completed), then try_wait,
+// which suspends the thread in hardware until the phase completes or a short
+// time limit passes, so it wakes as soon as the phase completes; at most
+// `limit` polls in all.  Only a wait far beyond any pipeline latency (2^14
+// polls) also sleeps between polls.  On timeout the shared abort word is set
+// and false returned; a wait that finds the word set gives up too, so every
+// role of the CTA stops its pipeline.  The default limit (~2^22 polls, a few
+// seconds) is far above any legitimate wait of these kernels.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
-                                          uint32_t limit = (1u << 22))
+                                          uint32_t limit = (1u << 22), uint32_t probes = 64u)
 {
-    const uint32_t probes = limit < 64u ? limit : 64u;
+    if (probes > limit) probes = limit;
     for (uint32_t f = 0; f < probes; ++f)
         if (mbar_test_wait(bar, parity)) return true;
     for (uint32_t i = probes; i < limit; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
-        if (i > 32) __nanosleep(i > 4096 ? 256 : 32);
+        if (i > (1u << 14)) __nanosleep(256);
     }
     *abort_flag = 1;
     return false;

@@ -126,10 +126,12 @@ __device__ __forceinline__ int units_per_pass(int nts)
 }
 
 // A wait of the filter's pipeline (see sm100::mbar_wait), bounded by the
-// poll limit set with irc_set_wait_limit.
+// poll limit set with irc_set_wait_limit.  It starts with try_wait (no
+// non-blocking probes): a probing warp would take issue slots from the
+// epilogue warps sharing its scheduler.
 __device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag)
 {
-    return sm100::mbar_wait(bar, parity, abort_flag, c_wait_polls);
+    return sm100::mbar_wait(bar, parity, abort_flag, c_wait_polls, 0u);
 }
 
 // Ascending bitonic sort of 32*PER keys held PER per lane (element e = lane*PER + i).
@@ -357,43 +359,7 @@ __device__ __forceinline__ void slot_barrier(int slot, int nthreads)
     asm volatile("bar.sync %0, %1;" ::"r"(1 + slot), "r"(nthreads) : "memory");
 }
 
-// Cursor over the 128-candidate tiles of one chunk: run r (absolute index), offset t.
 constexpr int TILE = 128;
-struct TileCursor {
-    // run bounds of the current run (rs, rn) and of the next one (ns, nn),
-    // loaded one run ahead so the loads are in flight while the current
-    // run's tiles are issued
-    int r, r0, r1, t, rs, rn, ns, nn;
-    __device__ __forceinline__ int after(int x) const { return x + 1 < r1 ? x + 1 : r0; }
-    __device__ __forceinline__ void reset(const irc::PlanDev &p, int chunk)
-    {
-        r0 = __ldg(p.roff + chunk);
-        r1 = __ldg(p.roff + chunk + 1);
-        r = r0;
-        t = 0;
-        rs = __ldg(p.rs + r);
-        rn = __ldg(p.rn + r);
-        const int n1 = after(r);
-        ns = __ldg(p.rs + n1);
-        nn = __ldg(p.rn + n1);
-    }
-    // current tile: first candidate row and valid column count; then advance
-    __device__ __forceinline__ void next(const irc::PlanDev &p, int &row0, int &ncol)
-    {
-        row0 = rs + t;
-        ncol = min(TILE, rn - t);
-        t += TILE;
-        if (t >= rn) {                                // next run; wraps for the second pass
-            t = 0;
-            r = after(r);
-            rs = ns;
-            rn = nn;
-            const int n1 = after(r);
-            ns = __ldg(p.rs + n1);
-            nn = __ldg(p.rn + n1);
-        }
-    }
-};
 
 __device__ __forceinline__ int chunk_tiles(const irc::PlanDev &p, int chunk)
 {
@@ -573,19 +539,31 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
     const int lb = bps == 4 ? 2 : bps == 2 ? 1 : 0;   // unit k is phase k / bps of its buffer's barriers
     const int U = units_per_pass<BN>(nts);
     bool ok = true;
-    TileCursor cur;
-    if (nts) cur.reset(p, it.chunk[s]);
+    // the slot's tile list: unit u is tile u (BN = 128) or tiles 2u, 2u + 1
+    // (BN = 256; the second is (0, 0) past the end of an odd count)
+    const int2 *tl = nts ? p.tc_tiles + __ldg(p.tc_toff + it.chunk[s]) : p.tc_tiles;
 
-    // Unit k: first row and valid count of this warp's columns in the unit's
-    // tile(s) (b: the second 128-tile of a 256-wide unit, none: nb = 0).
-    auto unit = [&](int k, int &ra, int &na, int &rb, int &nb) {
-        ra = na = rb = nb = 0;
-        cur.next(p, ra, na);
-        na -= part * PART;
-        if (BN == 256 && 2 * (k % U) + 1 < nts) {
-            cur.next(p, rb, nb);
-            nb -= part * PART;
+    // Unit k of the two passes: (first row, columns) of its tile(s), loaded
+    // one unit ahead of its use.
+    auto load_unit = [&](int k) -> int4 {
+        const int u = k < U ? k : k - U;
+        if constexpr (BN == 256) {
+            return __ldg(reinterpret_cast<const int4 *>(tl) + u);
+        } else {
+            const int2 v = __ldg(tl + u);
+            return make_int4(v.x, v.y, 0, 0);
         }
+    };
+    int4 cu = U ? load_unit(0) : make_int4(0, 0, 0, 0);
+    // this warp's columns of the unit: first rows ra, rb and valid counts na, nb
+    // of its 32 columns in each tile (none: <= 0)
+    auto unit = [&](int k, int &ra, int &na, int &rb, int &nb) {
+        const int4 nx = load_unit(k + 1 < 2 * U ? k + 1 : k);
+        ra = cu.x;
+        na = cu.y - part * PART;
+        rb = cu.z;
+        nb = cu.w - part * PART;
+        cu = nx;
     };
 
     // pass 1: per-column minima of this warp's columns
@@ -751,12 +729,12 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
         const int row0 = it.chunk[s] >= 0 ? it.qs[s] + (q % QPS) * 32 : 0;
         sm100::tma_load_2d(&tmQ, a_full, sA + q * (A_BYTES / 4), 0, row0);
     }
-    TileCursor cur[NS];
+    const int2 *tl[NS];
     int U[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         U[s] = units_per_pass<BN>(nt[s]);
-        if (nt[s]) cur[s].reset(p, it.chunk[s]);
+        tl[s] = nt[s] ? p.tc_tiles + __ldg(p.tc_toff + it.chunk[s]) : p.tc_tiles;
     }
     int i = 0;
     bool ok = true;
@@ -773,8 +751,7 @@ __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMa
                     const int nh = BN == 256 && 2 * u + 1 < nt[s] ? 2 : 1;   // 128-tiles of the unit
                     sm100::mbar_arrive_expect_tx(&full[st], nh * HALF_BYTES);
                     for (int h = 0; h < nh; ++h) {
-                        int row0, ncol;
-                        cur[s].next(p, row0, ncol);
+                        const int row0 = __ldg(tl[s] + (BN == 256 ? 2 * u + h : u)).x;
                         sm100::tma_load_2d(&tmC, &full[st], dst + h * HALF_BYTES, 0, row0);
                     }
                     ++i;
