@@ -212,8 +212,9 @@ size_t irc_plan_tc_bytes(const irc_plan *plan, int nC);
 int irc_plan_set_tc_buffer(irc_plan *plan, void *buf, size_t bytes);
 
 /* Poll limit of the tensor-core filter's pipeline waits on the current
- * device: polls > 0 sets it, polls <= 0 restores the default (~2^22 polls
- * with back-off, a few seconds).  A wait that runs out makes its CTA stop,
+ * device: polls > 0 sets it, polls <= 0 restores the default (2^22 polls,
+ * a few seconds).  A poll is a suspending try_wait; below 64 polls every poll
+ * is a non-blocking test instead.  A wait that runs out makes its CTA stop,
  * let its own copies and MMAs land, free its TMEM and set the plan's error
  * word, which irc_plan_check reports as IRC_E_TIMEOUT; a small limit
  * exercises that path.  Applies to later calls; not during stream capture.

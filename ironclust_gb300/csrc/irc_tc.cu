@@ -128,10 +128,13 @@ __device__ __forceinline__ int units_per_pass(int nts)
 // A wait of the filter's pipeline (see sm100::mbar_wait), bounded by the
 // poll limit set with irc_set_wait_limit.  It starts with try_wait (no
 // non-blocking probes): a probing warp would take issue slots from the
-// epilogue warps sharing its scheduler.
+// epilogue warps sharing its scheduler.  A limit below 64 polls makes every
+// poll a non-blocking test instead, so such a limit gives up at the first
+// phase that is not already complete (how the tests force the timeout path).
 __device__ __forceinline__ bool pipe_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag)
 {
-    return sm100::mbar_wait(bar, parity, abort_flag, c_wait_polls, 0u);
+    const uint32_t lim = c_wait_polls;
+    return sm100::mbar_wait(bar, parity, abort_flag, lim, lim < 64u ? lim : 0u);
 }
 
 // Ascending bitonic sort of 32*PER keys held PER per lane (element e = lane*PER + i).
