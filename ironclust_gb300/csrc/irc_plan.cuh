@@ -74,7 +74,8 @@ struct irc_plan {
     int32_t *scratch;                      // inside dmem: 4 words + 2 x n_out query lists
     const irc::TcItem *tc_items;           // tensor-core work items: inside dmem, or tc_items_buf
     int n_tc_items;
-    int n_tc_wide;                         // items [0, n_tc_wide) run on 256-candidate units, the rest on 128
+    int n_tc_one;                          // items [0, n_tc_one) have one slot, [n_tc_one, n_tc_wide) two
+    int n_tc_wide;                         // (both on 256-candidate units), the rest four (128-candidate units)
     void *tc_items_buf;                    // items of irc_plan_tc_layout, when called
     void *tc_buf;                          // tensor-core operand rows (2 x nF x tc_row_bytes) and the
                                            // padded FP32 rows of the re-rank, allocated lazily

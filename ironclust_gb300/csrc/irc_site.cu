@@ -163,7 +163,7 @@ struct Slot {
 // them in L2); order 1: chunk order.
 std::vector<irc::TcItem> build_tc_items(const int32_t *q0, const int32_t *nq, const int32_t *roff,
                                         const int32_t *rn, int nChunks, int max_slots, int order_mode,
-                                        int *n_wide)
+                                        int *n_one, int *n_wide)
 {
     std::vector<irc::TcItem> items;
     std::vector<int> cost;
@@ -211,17 +211,20 @@ std::vector<irc::TcItem> build_tc_items(const int32_t *q0, const int32_t *nq, co
     else
         std::stable_sort(order.begin(), order.end(),
                          [&](int a, int b) { return items[a].chunk[0] < items[b].chunk[0]; });
-    // items of one or two slots run on 256-candidate units (two 256-column
-    // accumulators), four-slot items on 128-candidate units (one accumulator
-    // per slot): the former first, each part in the order chosen above
-    std::stable_partition(order.begin(), order.end(), [&](int k) { return items[k].nslot <= 2; });
+    // one persistent launch per packing class: one-slot items, then two-slot
+    // items (both on 256-candidate units, two 256-column accumulators), then
+    // four-slot items (128-candidate units, one accumulator per slot), each
+    // class in the order chosen above
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return items[a].nslot < items[b].nslot; });
     std::vector<irc::TcItem> out;
     out.reserve(items.size());
-    int nw = 0;
+    int n1 = 0, nw = 0;
     for (int k : order) {
         out.push_back(items[k]);
+        n1 += items[k].nslot == 1;
         nw += items[k].nslot <= 2;
     }
+    *n_one = n1;
     *n_wide = nw;
     return out;
 }
@@ -453,8 +456,8 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     // tensor-core work items: 128-row tiles of large chunks, then the 33-64 and
     // 1-32 row remainders packed two and four per item (similar tile counts
     // together), all ordered by cost, largest first
-    int n_wide = 0;
-    std::vector<irc::TcItem> items = build_tc_items(q0, nq, moff.data(), mn.data(), nChunks, 4, 0, &n_wide);
+    int n_one = 0, n_wide = 0;
+    std::vector<irc::TcItem> items = build_tc_items(q0, nq, moff.data(), mn.data(), nChunks, 4, 0, &n_one, &n_wide);
     while (img.size() % 16) img.push_back(0);
     const size_t off_items = img.size();
     for (const irc::TcItem &it : items) {
@@ -494,6 +497,7 @@ int irc_plan_create(irc_plan **out, const int32_t *q0, const int32_t *nq, const 
     pl->scratch = (int32_t *)pl->dmem + img.size();
     pl->tc_items = reinterpret_cast<const irc::TcItem *>((const int32_t *)pl->dmem + off_items);
     pl->n_tc_items = (int)items.size();
+    pl->n_tc_one = n_one;
     pl->n_tc_wide = n_wide;
     e = cudaMemset(pl->scratch, 0, irc::kScratchLists * sizeof(int32_t));      // counters and error word
     if (e != cudaSuccess) { cudaFree(pl->dmem); free(pl); return irc_host::cuda_status(e, "irc_plan_create: clear"); }
@@ -551,9 +555,9 @@ int irc_plan_tc_layout(irc_plan *pl, int max_slots, int order)
     const int nChunks = pl->dev.nChunks;
     std::vector<int32_t> moff, ms, mn;
     merge_runs(pl->h_roff, pl->h_rs, pl->h_rn, nChunks, moff, ms, mn);
-    int n_wide = 0;
+    int n_one = 0, n_wide = 0;
     std::vector<irc::TcItem> items = build_tc_items(pl->h_q0, pl->h_nq, moff.data(), mn.data(), nChunks, max_slots,
-                                                    order, &n_wide);
+                                                    order, &n_one, &n_wide);
     void *buf = nullptr;
     cudaError_t e = cudaMalloc(&buf, sizeof(irc::TcItem) * (items.size() ? items.size() : 1));
     if (e == cudaSuccess)
@@ -566,6 +570,7 @@ int irc_plan_tc_layout(irc_plan *pl, int max_slots, int order)
     pl->tc_items_buf = buf;
     pl->tc_items = reinterpret_cast<const irc::TcItem *>(buf);
     pl->n_tc_items = (int)items.size();
+    pl->n_tc_one = n_one;
     pl->n_tc_wide = n_wide;
     return IRC_OK;
 }

@@ -1,12 +1,18 @@
 // irc_tc.cu -- tensor-core (tcgen05) site kNN: BF16 distance filter, exact
 // FP32 re-rank, FP64 at the k-th-neighbour boundary.
 //
-// A CTA serves one work item: up to four "slots", each a run of queries of
-// one drift chunk (128, 64 or 32 rows), packed into the 128 TMEM lanes of
-// one M=128 tile; every slot owns a share of the TMEM accumulators and its
-// own epilogue warps, and the slots' candidate tiles are issued round-robin
-// so small chunks (a probe site has ~17 queries per chunk) share a CTA
-// without waiting on each other.  Items are ordered by cost, largest first.
+// A work item is up to four "slots", each a run of queries of one drift
+// chunk (128, 64 or 32 rows), packed into the 128 TMEM lanes of one M=128
+// tile; every slot owns a share of the TMEM accumulators and its own epilogue
+// warps, and the slots' candidate tiles are issued round-robin so small
+// chunks (a probe site has ~17 queries per chunk) share a CTA without waiting
+// on each other.  The filter is persistent: one launch per packing class
+// (one-, two- or four-slot items), one CTA per SM, each CTA taking items from
+// the class's work queue (an atomic head over the items, ordered by cost,
+// largest first) until it is empty.  Barrier phases, stage and accumulator
+// counters run on across a CTA's items; the query tile is double-buffered,
+// so the next item's tiles load and its first MMAs run while the epilogue
+// still finishes the item before.
 // The BF16 (kind::f16) or FP8-e4m3 (kind::f8f6f4) operand rows of
 // irc_tc_host.cu -- 128 bytes each, so both use the same swizzled layout and
 // one MMA per 32 bytes -- make every accumulator the approximate squared
@@ -106,8 +112,9 @@ struct Tile {
     static constexpr int NBUF = TMEM_COLS / BN;   // accumulator buffers, split among the slots
     static constexpr int STAGES = BN == 256 ? 3 : 4;
     static constexpr uint32_t STAGE_BYTES = BN * KP * 2;
-    static constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + A_BYTES + (size_t)STAGE_BYTES * STAGES + LIST_BYTES +
-                                         BM * 4 /*tau*/ + BM * 4 /*counts*/ + 256;
+    // two query tiles (the next item's loads while this one's MMAs run)
+    static constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + 2 * A_BYTES + (size_t)STAGE_BYTES * STAGES +
+                                         LIST_BYTES + BM * 4 /*tau*/ + BM * 4 /*counts*/ + 256 /*barriers*/;
     static_assert(SMEM_BYTES <= 232448, "shared memory budget");
 };
 
@@ -516,163 +523,32 @@ __device__ __forceinline__ void append_hits(uint32_t *lrow, int *cnt, unsigned m
     }
 }
 
-// Epilogue of one warp: lane quarter `quarter` (the TMEM lanes it may read)
-// and part `part` (columns 32 * part .. 32 * part + 31 of every 128-tile of
-// its slot).  Each slot's epilogue warps synchronise only among themselves
-// (named barrier 1 + slot).
-template <int BN, bool TAU>
-__device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::TcItem &it, const int (&nt)[4], int qps,
-                                         int bps, int rank, uint32_t tmem, uint8_t *sA, int tau_k, uint32_t *lists,
-                                         float *sTau,
-                                         int *sCnt, uint64_t *acc_full, uint64_t *acc_empty, uint64_t *tau_ready,
-                                         volatile int *abort_flag, const irc_tc::ListOut &lo, int *scratch, int warp,
-                                         int lane)
+// Named barrier 1 + slot over the slot's epilogue warps that also returns the
+// AND of v over them: every warp of the slot gets the same answer, so they
+// leave the item loop together (a warp that left alone would leave the others
+// waiting at the slot's next barrier).
+__device__ __forceinline__ bool slot_barrier_and(int slot, int nthreads, bool v)
 {
-    const int ew = warp - 2;                      // 0..15
-    const int quarter = warp & 3;                 // TMEM lane quarter this warp may access
-    const int part = ew >> 2;                     // its 32 columns of every 128-tile
-    const int s = quarter / qps;                  // slot of this lane quarter
-    const int qrow = (quarter % qps) * 32;        // first row of this quarter inside its slot
-    const int nq_s = it.chunk[s] >= 0 ? it.nq[s] : 0;
-    const int nts = nt[s];
-    const int slot_threads = 32 * PARTS * qps;
-    const int row = quarter * 32 + lane;
-    const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + part * PART;
-    const bool active = qrow < nq_s;              // warp-uniform: any valid query in this quarter
-    const int lb = bps == 4 ? 2 : bps == 2 ? 1 : 0;   // unit k is phase k / bps of its buffer's barriers
-    const int U = units_per_pass<BN>(nts);
-    bool ok = true;
-    // the slot's tile list: unit u is tile u (BN = 128) or tiles 2u, 2u + 1
-    // (BN = 256; the second is (0, 0) past the end of an odd count)
-    const int2 *tl = nts ? p.tc_tiles + __ldg(p.tc_toff + it.chunk[s]) : p.tc_tiles;
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + slot), "r"(nthreads)
+        : "memory");
+    return r != 0;
+}
 
-    // Unit k of the two passes: (first row, columns) of its tile(s), loaded
-    // one unit ahead of its use.
-    auto load_unit = [&](int k) -> int4 {
-        const int u = k < U ? k : k - U;
-        if constexpr (BN == 256) {
-            return __ldg(reinterpret_cast<const int4 *>(tl) + u);
-        } else {
-            const int2 v = __ldg(tl + u);
-            return make_int4(v.x, v.y, 0, 0);
-        }
-    };
-    int4 cu = U ? load_unit(0) : make_int4(0, 0, 0, 0);
-    // this warp's columns of the unit: first rows ra, rb and valid counts na, nb
-    // of its 32 columns in each tile (none: <= 0)
-    auto unit = [&](int k, int &ra, int &na, int &rb, int &nb) {
-        const int4 nx = load_unit(k + 1 < 2 * U ? k + 1 : k);
-        ra = cu.x;
-        na = cu.y - part * PART;
-        rb = cu.z;
-        nb = cu.w - part * PART;
-        cu = nx;
-    };
-
-    // pass 1: per-column minima of this warp's columns
-    float bm[PART];
-#pragma unroll
-    for (int c = 0; c < PART; ++c) bm[c] = __int_as_float(0x7f800000);
-    for (int k = 0; k < U && ok; ++k) {
-        int ra, na, rb, nb;
-        unit(k, ra, na, rb, nb);
-        const int b = s * bps + (k & (bps - 1));
-        if (!(ok = pipe_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
-        sm100::tc_fence_after();
-        if (active) {
-            if constexpr (BN == 256) {
-                // either tile may be the short one (the first when it ends a run)
-                if (na > 0 || nb > 0) fold2x32(tbase + b * BN, na, tbase + b * BN + 128, nb, bm);
-            } else {
-                if (na > 0) fold32(tbase + b * BN, na, bm);
-            }
-        }
-        sm100::tc_fence_before();
-        __syncwarp();
-        if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
-    }
-    // threshold: rank-th smallest of the 128 column minima of every query; the
-    // minima rows of a quarter alias that quarter's own list rows
-    float *qarea = reinterpret_cast<float *>(lists + (size_t)quarter * 32 * LROW);
-    {
-        float *brow = qarea + lane * BROW + part * PART;
-#pragma unroll
-        for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
-        if (part == 0) sCnt[row] = 0;             // list counts of pass 2 (ordered by the barriers below)
-        slot_barrier(s, slot_threads);
-        // The warp's 8 rows at once (independent chains): a bitwise search,
-        // from the top, of the largest t with fewer than 64 minima below it,
-        // i.e. of the rank-th smallest minimum, on the non-negative float bit
-        // patterns.  It stops at TAU_LOW_BIT and rounds up, so tau is an
-        // upper bound of the rank-th smallest within 2^-11 of it (a few more
-        // candidates listed, never fewer).
-        constexpr int RL = 32 / PARTS;
-        unsigned v4[RL][4], ans[RL];
-#pragma unroll
-        for (int L = 0; L < RL; ++L) {
-            const float *bl = qarea + (part * RL + L) * BROW;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) v4[L][u] = __float_as_uint(bl[u * 32 + lane]);
-            ans[L] = 0u;
-        }
-#pragma unroll 1
-        for (int b = 30; b >= TAU_LOW_BIT; --b) {
-#pragma unroll
-            for (int L = 0; L < RL; ++L) {
-                const unsigned t = ans[L] | (1u << b);
-                const unsigned c = (unsigned)(v4[L][0] < t) + (unsigned)(v4[L][1] < t) + (unsigned)(v4[L][2] < t) +
-                                   (unsigned)(v4[L][3] < t);
-                if (__reduce_add_sync(0xffffffffu, c) < (unsigned)rank) ans[L] = t;
-            }
-        }
-        if (lane < RL) {
-            unsigned a = ans[0];
-#pragma unroll
-            for (int L = 1; L < RL; ++L)
-                if (lane == L) a = ans[L];
-            sTau[quarter * 32 + part * RL + lane] = __uint_as_float(min(a | ((1u << TAU_LOW_BIT) - 1u), 0x7f800000u));
-        }
-        slot_barrier(s, slot_threads);     // minima rows are read; the list rows may be written
-    }
-    const float tau = sTau[row];
-    if (TAU && part == 0) {
-        // the thresholds into the query tile; visible to the tensor core
-        // (async proxy) before the MMA thread, released by tau_ready, issues
-        // the slot's pass-2 MMAs
-        put_tau(sA, row, tau_k, tau);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncwarp();
-        if (lane == 0) sm100::mbar_arrive(&tau_ready[s]);
-    }
-    // pass 2: collect the candidates at or below tau
-    uint32_t *lrow = lists + (size_t)row * LROW;
-    for (int k = U; k < 2 * U && ok; ++k) {
-        int ra, na, rb, nb;
-        unit(k, ra, na, rb, nb);
-        const int b = s * bps + (k & (bps - 1));
-        if (!(ok = pipe_wait(&acc_full[b], (k >> lb) & 1, abort_flag))) break;
-        sm100::tc_fence_after();
-        if (active && (na > 0 || nb > 0)) {
-            unsigned ma = 0u, mb = 0u;
-            if constexpr (BN == 256 && TAU) {
-                mark2x32_signs(tbase + b * BN, na, tbase + b * BN + 128, nb, ma, mb);
-            } else {
-                if (na > 0) ma = mark32(tbase + b * BN, na, tau);
-                if (BN == 256 && nb > 0) mb = mark32(tbase + b * BN + 128, nb, tau);
-            }
-            if (ma) append_hits(lrow, sCnt + row, ma, (uint32_t)(ra + part * PART));
-            if (mb) append_hits(lrow, sCnt + row, mb, (uint32_t)(rb + part * PART));
-        }
-        sm100::tc_fence_before();
-        __syncwarp();
-        if (lane == 0) sm100::mbar_arrive(&acc_empty[b]);
-    }
-    slot_barrier(s, slot_threads);
-    // Hand the lists to the re-rank kernel: this warp packs 8 of its
-    // quarter's queries (query L in lane L) into one bump allocation and
-    // records (offset, length) per query; a list past LISTCAP or a full list
-    // area sends the query to the exact fallback instead.
-    if (!__all_sync(0xffffffffu, ok)) return;
+// The handoff of one item's lists to the re-rank kernel: this warp packs 8 of
+// its quarter's queries (query L in lane L) into one bump allocation and
+// records (offset, length) per query; a list past LISTCAP or a full list area
+// sends the query to the exact fallback instead.
+__device__ __forceinline__ void hand_off(const irc::PlanDev &p, const irc_tc::TcItem &it, int s, int quarter, int part,
+                                         int qrow, int nq_s, const uint32_t *lists, const int *sCnt,
+                                         const irc_tc::ListOut &lo, int *scratch, int lane)
+{
     constexpr int RL = 32 / PARTS;
     int cL = -1;                                  // -1: no query in this lane, -2: to the fallback
     if (lane < RL && qrow + part * RL + lane < nq_s) {
@@ -713,101 +589,323 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
     }
 }
 
-// TMA producer (one thread): the four 32-row query boxes, then the slots'
-// units round-robin, each slot's sequence twice (both passes).  A unit's
-// 128-candidate tiles land in consecutive 128-row halves of its stage.
+// Shared state of a persistent filter CTA: the item ring (the producer claims
+// items from the launch's work queue and publishes their indices), the
+// double-buffered query tile and the mbarriers of every stage.
+struct Shared {
+    uint8_t *sA;                                  // two query tiles, A_BYTES each
+    uint8_t *sB;                                  // candidate stages
+    uint32_t *lists;                              // [BM][LROW]
+    float *sTau;                                  // [BM]
+    int *sCnt;                                    // [BM] list counts
+    uint64_t *full, *empty;                       // [STAGES] candidate stages loaded / consumed
+    uint64_t *a_full, *a_empty;                   // [2] query tile loaded / its item's MMAs done
+    uint64_t *acc_full, *acc_empty;               // [NBUF] accumulator written / read
+    uint64_t *tau_ready;                          // [4] a slot's thresholds are in its query tile
+    uint64_t *item_full, *item_empty;             // [2] item index published / read by every consumer
+    uint64_t *mma_done;
+    int *item_idx;                                // [2]
+    uint32_t *tmem_slot;
+    volatile int *abort_flag;
+};
+
+// Epilogue of one warp: lane quarter `quarter` (the TMEM lanes it may read)
+// and part `part` (columns 32 * part .. 32 * part + 31 of every 128-tile of
+// its slot), over the items the CTA takes.  Each slot's epilogue warps
+// synchronise only among themselves (named barrier 1 + slot).  Unit g of a
+// slot (counted over all its items, both passes) goes to accumulator
+// s * BPS + g % BPS, whose barriers are in phase g / BPS.
+template <int BN, int NS, bool TAU>
+__device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::TcItem *__restrict__ items, int rank,
+                                         uint32_t tmem, int tau_k, const Shared &sh, const irc_tc::ListOut &lo,
+                                         int *scratch, int warp, int lane)
+{
+    using T = Tile<BN>;
+    constexpr int QPS = 4 / NS;                   // lane quarters per slot
+    constexpr int BPS = T::NBUF / NS;             // accumulator buffers per slot
+    const int ew = warp - 2;                      // 0..15
+    const int quarter = warp & 3;                 // TMEM lane quarter this warp may access
+    const int part = ew >> 2;                     // its 32 columns of every 128-tile
+    const int s = quarter / QPS;                  // slot of this lane quarter
+    const int qrow = (quarter % QPS) * 32;        // first row of this quarter inside its slot
+    const int slot_threads = 32 * PARTS * QPS;
+    const int row = quarter * 32 + lane;
+    const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + part * PART;
+    // the minima rows of a quarter alias that quarter's own list rows
+    float *qarea = reinterpret_cast<float *>(sh.lists + (size_t)quarter * 32 * LROW);
+    uint32_t *lrow = sh.lists + (size_t)row * LROW;
+    unsigned g0 = 0;                              // this slot's units of the earlier items
+    for (int seq = 0;; ++seq) {
+        const int r = seq & 1;
+        bool ok = pipe_wait(&sh.item_full[r], (seq >> 1) & 1, sh.abort_flag);
+        if (!slot_barrier_and(s, slot_threads, ok)) break;
+        const int idx = sh.item_idx[r];
+        __syncwarp();
+        if (lane == 0) sm100::mbar_arrive(&sh.item_empty[r]);
+        if (idx < 0) break;                       // the queue is empty
+        const irc_tc::TcItem it = items[idx];
+        const int nq_s = it.chunk[s] >= 0 ? it.nq[s] : 0;
+        const int nts = chunk_tiles(p, it.chunk[s]);
+        const bool active = qrow < nq_s;          // warp-uniform: any valid query in this quarter
+        const int U = units_per_pass<BN>(nts);
+        // the slot's tile list: unit u is tile u (BN = 128) or tiles 2u, 2u + 1
+        // (BN = 256; the second is (0, 0) past the end of an odd count)
+        const int2 *tl = nts ? p.tc_tiles + __ldg(p.tc_toff + it.chunk[s]) : p.tc_tiles;
+
+        // Unit k of the two passes: (first row, columns) of its tile(s), loaded
+        // one unit ahead of its use.
+        auto load_unit = [&](int k) -> int4 {
+            const int u = k < U ? k : k - U;
+            if constexpr (BN == 256) {
+                return __ldg(reinterpret_cast<const int4 *>(tl) + u);
+            } else {
+                const int2 v = __ldg(tl + u);
+                return make_int4(v.x, v.y, 0, 0);
+            }
+        };
+        int4 cu = U ? load_unit(0) : make_int4(0, 0, 0, 0);
+        // this warp's columns of the unit: first rows ra, rb and valid counts
+        // na, nb of its 32 columns in each tile (none: <= 0)
+        auto unit = [&](int k, int &ra, int &na, int &rb, int &nb) {
+            const int4 nx = load_unit(k + 1 < 2 * U ? k + 1 : k);
+            ra = cu.x;
+            na = cu.y - part * PART;
+            rb = cu.z;
+            nb = cu.w - part * PART;
+            cu = nx;
+        };
+
+        // pass 1: per-column minima of this warp's columns
+        float bm[PART];
+#pragma unroll
+        for (int c = 0; c < PART; ++c) bm[c] = __int_as_float(0x7f800000);
+        for (int k = 0; k < U && ok; ++k) {
+            int ra, na, rb, nb;
+            unit(k, ra, na, rb, nb);
+            const unsigned g = g0 + (unsigned)k;
+            const int b = s * BPS + (int)(g % BPS);
+            if (!(ok = pipe_wait(&sh.acc_full[b], (g / BPS) & 1, sh.abort_flag))) break;
+            sm100::tc_fence_after();
+            if (active) {
+                if constexpr (BN == 256) {
+                    // either tile may be the short one (the first when it ends a run)
+                    if (na > 0 || nb > 0) fold2x32(tbase + b * BN, na, tbase + b * BN + 128, nb, bm);
+                } else {
+                    if (na > 0) fold32(tbase + b * BN, na, bm);
+                }
+            }
+            sm100::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) sm100::mbar_arrive(&sh.acc_empty[b]);
+        }
+        // threshold: rank-th smallest of the 128 column minima of every query
+        {
+            float *brow = qarea + lane * BROW + part * PART;
+#pragma unroll
+            for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
+            if (part == 0) sh.sCnt[row] = 0;                 // list counts of pass 2 (ordered by the barriers below)
+            slot_barrier(s, slot_threads);
+            // The warp's 8 rows at once (independent chains): a bitwise
+            // search, from the top, of the largest t with fewer than rank
+            // minima below it, i.e. of the rank-th smallest minimum, on the
+            // non-negative float bit patterns.  It stops at TAU_LOW_BIT and
+            // rounds up, so tau is an upper bound of the rank-th smallest
+            // within 2^-11 of it (a few more candidates listed, never fewer).
+            constexpr int RL = 32 / PARTS;
+            unsigned v4[RL][4], ans[RL];
+#pragma unroll
+            for (int L = 0; L < RL; ++L) {
+                const float *bl = qarea + (part * RL + L) * BROW;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v4[L][u] = __float_as_uint(bl[u * 32 + lane]);
+                ans[L] = 0u;
+            }
+#pragma unroll 1
+            for (int b = 30; b >= TAU_LOW_BIT; --b) {
+#pragma unroll
+                for (int L = 0; L < RL; ++L) {
+                    const unsigned t = ans[L] | (1u << b);
+                    const unsigned c = (unsigned)(v4[L][0] < t) + (unsigned)(v4[L][1] < t) +
+                                       (unsigned)(v4[L][2] < t) + (unsigned)(v4[L][3] < t);
+                    if (__reduce_add_sync(0xffffffffu, c) < (unsigned)rank) ans[L] = t;
+                }
+            }
+            if (lane < RL) {
+                unsigned a = ans[0];
+#pragma unroll
+                for (int L = 1; L < RL; ++L)
+                    if (lane == L) a = ans[L];
+                sh.sTau[quarter * 32 + part * RL + lane] =
+                    __uint_as_float(min(a | ((1u << TAU_LOW_BIT) - 1u), 0x7f800000u));
+            }
+            slot_barrier(s, slot_threads);        // minima rows are read; the list rows may be written
+        }
+        const float tau = sh.sTau[row];
+        if (TAU && part == 0 && U > 0) {
+            // the thresholds into the item's query tile; visible to the tensor
+            // core (async proxy) before the MMA thread, released by tau_ready,
+            // issues the slot's pass-2 MMAs (one phase per item with units)
+            put_tau(sh.sA + (size_t)r * A_BYTES, row, tau_k, tau);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) sm100::mbar_arrive(&sh.tau_ready[s]);
+        }
+        // pass 2: collect the candidates at or below tau
+        for (int k = U; k < 2 * U && ok; ++k) {
+            int ra, na, rb, nb;
+            unit(k, ra, na, rb, nb);
+            const unsigned g = g0 + (unsigned)k;
+            const int b = s * BPS + (int)(g % BPS);
+            if (!(ok = pipe_wait(&sh.acc_full[b], (g / BPS) & 1, sh.abort_flag))) break;
+            sm100::tc_fence_after();
+            if (active && (na > 0 || nb > 0)) {
+                unsigned ma = 0u, mb = 0u;
+                if constexpr (BN == 256 && TAU) {
+                    mark2x32_signs(tbase + b * BN, na, tbase + b * BN + 128, nb, ma, mb);
+                } else {
+                    if (na > 0) ma = mark32(tbase + b * BN, na, tau);
+                    if (BN == 256 && nb > 0) mb = mark32(tbase + b * BN + 128, nb, tau);
+                }
+                if (ma) append_hits(lrow, sh.sCnt + row, ma, (uint32_t)(ra + part * PART));
+                if (mb) append_hits(lrow, sh.sCnt + row, mb, (uint32_t)(rb + part * PART));
+            }
+            sm100::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) sm100::mbar_arrive(&sh.acc_empty[b]);
+        }
+        slot_barrier(s, slot_threads);
+        if (__all_sync(0xffffffffu, ok)) hand_off(p, it, s, quarter, part, qrow, nq_s, sh.lists, sh.sCnt, lo, scratch, lane);
+        g0 += 2u * (unsigned)U;
+        // every warp of the slot is done with this item's lists before the
+        // next item's minima overwrite them; after a timed-out wait all stop
+        if (!slot_barrier_and(s, slot_threads, ok && !*sh.abort_flag)) break;
+    }
+}
+
+// TMA producer (one thread): claims items from the launch's work queue and
+// publishes their indices (a two-entry ring), loads each item's four 32-row
+// query boxes into the free query tile, then the slots' units round-robin,
+// each slot's sequence twice (both passes).  A unit's 128-candidate tiles land
+// in consecutive 128-row halves of its stage.  Stage and tile counters run on
+// across items, so the ring never drains between them.
 template <int BN, int NS>
 __device__ __forceinline__ void produce(const CUtensorMap &tmQ, const CUtensorMap &tmC, const irc::PlanDev &p,
-                                        const irc_tc::TcItem &it, const int (&nt)[4], uint8_t *sA, uint8_t *sB,
-                                        uint64_t *full, uint64_t *empty, uint64_t *a_full, volatile int *abort_flag)
+                                        const irc_tc::TcItem *__restrict__ items, int n_items, unsigned *queue,
+                                        const Shared &sh)
 {
     using T = Tile<BN>;
     constexpr int QPS = 4 / NS;
     sm100::prefetch_tmap(&tmQ);
     sm100::prefetch_tmap(&tmC);
-    sm100::mbar_arrive_expect_tx(a_full, A_BYTES);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int s = q / QPS;
-        const int row0 = it.chunk[s] >= 0 ? it.qs[s] + (q % QPS) * 32 : 0;
-        sm100::tma_load_2d(&tmQ, a_full, sA + q * (A_BYTES / 4), 0, row0);
-    }
-    const int2 *tl[NS];
-    int U[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        U[s] = units_per_pass<BN>(nt[s]);
-        tl[s] = nt[s] ? p.tc_tiles + __ldg(p.tc_toff + it.chunk[s]) : p.tc_tiles;
-    }
-    int i = 0;
+    int i = 0, n_a = 0;                           // candidate stages and query tiles loaded
     bool ok = true;
-    for (int k = 0; ok; ++k) {
-        bool any = false;
+    for (int seq = 0; ok; ++seq) {
+        const int r = seq & 1;
+        const unsigned claim = atomicAdd(queue, 1u);
+        const int idx = claim < (unsigned)n_items ? (int)claim : -1;
+        if (!(ok = pipe_wait(&sh.item_empty[r], ((seq >> 1) & 1) ^ 1, sh.abort_flag))) break;
+        sh.item_idx[r] = idx;
+        sm100::mbar_arrive(&sh.item_full[r]);     // release: the index is visible to the waiters
+        if (idx < 0) break;
+        const irc_tc::TcItem it = items[idx];
+        const int2 *tl[NS];
+        int U[NS], nt[NS];
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-            if (ok && k < 2 * U[s]) {
-                any = true;
-                const int u = k % U[s];
-                const int st = i % T::STAGES;
-                if ((ok = pipe_wait(&empty[st], ((i / T::STAGES) & 1) ^ 1, abort_flag))) {
-                    uint8_t *dst = sB + (size_t)st * T::STAGE_BYTES;
-                    const int nh = BN == 256 && 2 * u + 1 < nt[s] ? 2 : 1;   // 128-tiles of the unit
-                    sm100::mbar_arrive_expect_tx(&full[st], nh * HALF_BYTES);
-                    for (int h = 0; h < nh; ++h) {
-                        const int row0 = __ldg(tl[s] + (BN == 256 ? 2 * u + h : u)).x;
-                        sm100::tma_load_2d(&tmC, &full[st], dst + h * HALF_BYTES, 0, row0);
-                    }
-                    ++i;
-                }
-            }
+            nt[s] = chunk_tiles(p, it.chunk[s]);
+            U[s] = units_per_pass<BN>(nt[s]);
+            tl[s] = nt[s] ? p.tc_tiles + __ldg(p.tc_toff + it.chunk[s]) : p.tc_tiles;
         }
-        if (!any) break;
-    }
-    // every issued load has landed before the CTA exits
-    for (int j = (i > T::STAGES ? i - T::STAGES : 0); j < i; ++j)
-        sm100::mbar_drain(&full[j % T::STAGES], (j / T::STAGES) & 1);
-    sm100::mbar_drain(a_full, 0);
-}
-
-// MMA issuer (one thread), in the producer's order; slot s's unit k goes to
-// accumulator s*BPS + k % BPS and is issued once every epilogue warp of the
-// slot released the previous unit in that buffer (k - BPS).  With TAU the
-// slot's first pass-2 unit also waits until its epilogue wrote the
-// thresholds into the query tile (tau_ready[s]).
-template <int BN, int NS, bool FP8, bool TAU>
-__device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem, uint8_t *sA,
-                                      uint8_t *sB, uint64_t *full, uint64_t *empty, uint64_t *a_full,
-                                      uint64_t *acc_full, uint64_t *acc_empty, uint64_t *tau_ready, uint64_t *mma_done,
-                                      volatile int *abort_flag)
-{
-    using T = Tile<BN>;
-    constexpr int BPS = T::NBUF / NS;
-    // bf16 x bf16 (kind::f16, K = 16) or e4m3 x e4m3 (kind::f8f6f4, K = 32) -> f32;
-    // either way one MMA consumes 32 bytes of every 128-byte operand row
-    constexpr uint32_t idesc = FP8 ? sm100::idesc_make(BM, BN, 0, 0) : sm100::idesc_make(BM, BN, 1, 1);
-    if (pipe_wait(a_full, 0, abort_flag)) {
-        sm100::tc_fence_after();
-        const uint64_t adesc = sm100::sdesc_sw128(sm100::smem_u32(sA));
-        int U[NS];
+        // the query tile of item seq - 2 is free once that item's MMAs are done
+        if (!(ok = pipe_wait(&sh.a_empty[r], ((seq >> 1) & 1) ^ 1, sh.abort_flag))) break;
+        uint8_t *sA = sh.sA + (size_t)r * A_BYTES;
+        sm100::mbar_arrive_expect_tx(&sh.a_full[r], A_BYTES);
 #pragma unroll
-        for (int s = 0; s < NS; ++s) U[s] = units_per_pass<BN>(nt[s]);
-        int i = 0;
-        bool ok = true;
+        for (int q = 0; q < 4; ++q) {
+            const int s = q / QPS;
+            const int row0 = it.chunk[s] >= 0 ? it.qs[s] + (q % QPS) * 32 : 0;
+            sm100::tma_load_2d(&tmQ, &sh.a_full[r], sA + q * (A_BYTES / 4), 0, row0);
+        }
+        ++n_a;
         for (int k = 0; ok; ++k) {
             bool any = false;
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
                 if (ok && k < 2 * U[s]) {
                     any = true;
-                    const int b = s * BPS + k % BPS, st = i % T::STAGES;
-                    ok = (k < BPS || pipe_wait(&acc_empty[b], ((k - BPS) / BPS) & 1, abort_flag)) &&
-                         pipe_wait(&full[st], (i / T::STAGES) & 1, abort_flag) &&
+                    const int u = k % U[s];
+                    const int st = i % T::STAGES;
+                    if ((ok = pipe_wait(&sh.empty[st], ((i / T::STAGES) & 1) ^ 1, sh.abort_flag))) {
+                        uint8_t *dst = sh.sB + (size_t)st * T::STAGE_BYTES;
+                        const int nh = BN == 256 && 2 * u + 1 < nt[s] ? 2 : 1;   // 128-tiles of the unit
+                        sm100::mbar_arrive_expect_tx(&sh.full[st], nh * HALF_BYTES);
+                        for (int h = 0; h < nh; ++h) {
+                            const int row0 = __ldg(tl[s] + (BN == 256 ? 2 * u + h : u)).x;
+                            sm100::tma_load_2d(&tmC, &sh.full[st], dst + h * HALF_BYTES, 0, row0);
+                        }
+                        ++i;
+                    }
+                }
+            }
+            if (!any) break;
+        }
+    }
+    // every issued load has landed before the CTA exits
+    for (int j = (i > T::STAGES ? i - T::STAGES : 0); j < i; ++j)
+        sm100::mbar_drain(&sh.full[j % T::STAGES], (j / T::STAGES) & 1);
+    for (int j = (n_a > 2 ? n_a - 2 : 0); j < n_a; ++j) sm100::mbar_drain(&sh.a_full[j & 1], (j >> 1) & 1);
+}
+
+// MMA issuer (one thread), in the producer's order; unit g of slot s (counted
+// over the CTA's items) goes to accumulator s*BPS + g % BPS and is issued once
+// every epilogue warp of the slot released unit g - BPS of that buffer.  With
+// TAU the slot's first pass-2 unit of an item also waits until its epilogue
+// wrote the thresholds into the query tile (tau_ready[s], one phase per item
+// in which the slot has units).  After an item's last MMA a commit frees its
+// query tile.
+template <int BN, int NS, bool FP8, bool TAU>
+__device__ __forceinline__ void issue(const irc::PlanDev &p, const irc_tc::TcItem *__restrict__ items, int nk,
+                                      uint32_t tmem, const Shared &sh)
+{
+    using T = Tile<BN>;
+    constexpr int BPS = T::NBUF / NS;
+    // bf16 x bf16 (kind::f16, K = 16) or e4m3 x e4m3 (kind::f8f6f4, K = 32) -> f32;
+    // either way one MMA consumes 32 bytes of every 128-byte operand row
+    constexpr uint32_t idesc = FP8 ? sm100::idesc_make(BM, BN, 0, 0) : sm100::idesc_make(BM, BN, 1, 1);
+    unsigned g0[NS], taus[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) g0[s] = taus[s] = 0;
+    int i = 0;
+    bool ok = true;
+    for (int seq = 0; ok; ++seq) {
+        const int r = seq & 1;
+        if (!(ok = pipe_wait(&sh.item_full[r], (seq >> 1) & 1, sh.abort_flag))) break;
+        const int idx = sh.item_idx[r];
+        sm100::mbar_arrive(&sh.item_empty[r]);
+        if (idx < 0) break;
+        const irc_tc::TcItem it = items[idx];
+        int U[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) U[s] = units_per_pass<BN>(chunk_tiles(p, it.chunk[s]));
+        if (!(ok = pipe_wait(&sh.a_full[r], (seq >> 1) & 1, sh.abort_flag))) break;
+        sm100::tc_fence_after();
+        const uint64_t adesc = sm100::sdesc_sw128(sm100::smem_u32(sh.sA + (size_t)r * A_BYTES));
+        for (int k = 0; ok; ++k) {
+            bool any = false;
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                if (ok && k < 2 * U[s]) {
+                    any = true;
+                    const unsigned g = g0[s] + (unsigned)k, use = g / BPS;
+                    const int b = s * BPS + (int)(g % BPS), st = i % T::STAGES;
+                    ok = (use == 0 || pipe_wait(&sh.acc_empty[b], (use - 1) & 1, sh.abort_flag)) &&
+                         pipe_wait(&sh.full[st], (i / T::STAGES) & 1, sh.abort_flag) &&
                          // the slot's thresholds are in the query tile before its pass 2
-                         (!TAU || k != U[s] || pipe_wait(&tau_ready[s], 0, abort_flag));
+                         (!TAU || k != U[s] || pipe_wait(&sh.tau_ready[s], taus[s] & 1, sh.abort_flag));
                     if (ok) {
                         sm100::tc_fence_after();
                         const uint64_t bdesc =
-                            sm100::sdesc_sw128(sm100::smem_u32(sB + (size_t)st * T::STAGE_BYTES));
+                            sm100::sdesc_sw128(sm100::smem_u32(sh.sB + (size_t)st * T::STAGE_BYTES));
 #pragma unroll
                         for (int kk = 0; kk < KP / 16; ++kk)
                             if (kk >= nk)
@@ -816,106 +914,96 @@ __device__ __forceinline__ void issue(const int (&nt)[4], int nk, uint32_t tmem,
                                 sm100::mma_f8(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
                             else
                                 sm100::mma_f16(tmem + b * BN, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk > 0 ? 1u : 0u);
-                        sm100::mma_commit(&empty[st]);
-                        sm100::mma_commit(&acc_full[b]);
+                        sm100::mma_commit(&sh.empty[st]);
+                        sm100::mma_commit(&sh.acc_full[b]);
                         ++i;
                     }
                 }
             }
             if (!any) break;
         }
+        if (!ok) break;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            g0[s] += 2u * (unsigned)U[s];
+            taus[s] += U[s] > 0 ? 1u : 0u;
+        }
+        sm100::mma_commit(&sh.a_empty[r]);        // this item's MMAs done: its query tile may be replaced
     }
     // every MMA has completed before TMEM is released
-    sm100::mma_commit(mma_done);
-    sm100::mbar_drain(mma_done, 0);
+    sm100::mma_commit(sh.mma_done);
+    sm100::mbar_drain(sh.mma_done, 0);
 }
 
-// The filter over the work items of one unit width (items of one or two slots
-// at BN = 256, four-slot items at BN = 128); TAU: pass 2 reads the signs of
-// d2 - tau (the thresholds written into the query tile at K position tau_k),
-// else it compares d2 with tau in the epilogue.
-template <bool FP8, int BN, bool TAU>
+// The filter over the work items of one packing class (NS slots per item:
+// one or two at BN = 256, four at BN = 128), persistent: each CTA takes items
+// from the class's work queue (queue: its head, items cost-ordered) until it
+// is empty.  TAU: pass 2 reads the signs of d2 - tau (the thresholds written
+// into the query tile at K position tau_k), else it compares d2 with tau in
+// the epilogue.
+template <bool FP8, int BN, bool TAU, int NS>
 __global__ void __launch_bounds__(THREADS, 1)
 k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmC, irc::PlanDev p,
-         const irc_tc::TcItem *__restrict__ items, int nk, int tau_k, irc_tc::ListOut lo, int *__restrict__ scratch)
+         const irc_tc::TcItem *__restrict__ items, int n_items, unsigned *queue, int nk, int tau_k, irc_tc::ListOut lo,
+         int *__restrict__ scratch)
 {
     using T = Tile<BN>;
+    constexpr int QPS = 4 / NS;
     extern __shared__ unsigned char smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t *sA = base;
-    uint8_t *sB = base + A_BYTES;
-    uint32_t *lists = reinterpret_cast<uint32_t *>(sB + T::STAGES * T::STAGE_BYTES);   // [BM][LROW]
-    float *sTau = reinterpret_cast<float *>(lists + (size_t)LROW * BM);              // [BM]
-    int *sCnt = reinterpret_cast<int *>(sTau + BM);                                  // [BM] list counts
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sCnt + BM);
-    uint64_t *full = bars, *empty = bars + T::STAGES, *a_full = bars + 2 * T::STAGES;
-    uint64_t *acc_full = a_full + 1, *acc_empty = acc_full + T::NBUF;
-    uint64_t *mma_done = acc_empty + T::NBUF;
-    uint64_t *tau_ready = mma_done + 1;                                              // [4], one per slot
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tau_ready + 4);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    Shared sh;
+    sh.sA = base;
+    sh.sB = base + 2 * A_BYTES;
+    sh.lists = reinterpret_cast<uint32_t *>(sh.sB + T::STAGES * T::STAGE_BYTES);   // [BM][LROW]
+    sh.sTau = reinterpret_cast<float *>(sh.lists + (size_t)LROW * BM);
+    sh.sCnt = reinterpret_cast<int *>(sh.sTau + BM);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sh.sCnt + BM);
+    sh.full = bars;
+    sh.empty = sh.full + T::STAGES;
+    sh.a_full = sh.empty + T::STAGES;
+    sh.a_empty = sh.a_full + 2;
+    sh.acc_full = sh.a_empty + 2;
+    sh.acc_empty = sh.acc_full + T::NBUF;
+    sh.tau_ready = sh.acc_empty + T::NBUF;
+    sh.item_full = sh.tau_ready + 4;
+    sh.item_empty = sh.item_full + 2;
+    sh.mma_done = sh.item_empty + 2;
+    sh.item_idx = reinterpret_cast<int *>(sh.mma_done + 1);
+    sh.tmem_slot = reinterpret_cast<uint32_t *>(sh.item_idx + 2);
+    sh.abort_flag = reinterpret_cast<volatile int *>(sh.tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const irc_tc::TcItem it = items[blockIdx.x];
-    const int nslot = it.nslot, qps = 4 / nslot, bps = T::NBUF / nslot;
-    int nt[4];
-#pragma unroll
-    for (int s = 0; s < 4; ++s) nt[s] = s < nslot ? chunk_tiles(p, it.chunk[s]) : 0;    // 128-tiles
-
     if (threadIdx.x == 0) {
-        for (int s = 0; s < T::STAGES; ++s) { sm100::mbar_init(&full[s], 1); sm100::mbar_init(&empty[s], 1); }
-        sm100::mbar_init(a_full, 1);
-        for (int b = 0; b < T::NBUF; ++b) {
-            sm100::mbar_init(&acc_full[b], 1);
-            sm100::mbar_init(&acc_empty[b], PARTS * qps);       // the slot's epilogue warps
+        for (int s = 0; s < T::STAGES; ++s) { sm100::mbar_init(&sh.full[s], 1); sm100::mbar_init(&sh.empty[s], 1); }
+        for (int r = 0; r < 2; ++r) {
+            sm100::mbar_init(&sh.a_full[r], 1);
+            sm100::mbar_init(&sh.a_empty[r], 1);
+            sm100::mbar_init(&sh.item_full[r], 1);
+            sm100::mbar_init(&sh.item_empty[r], 1 + EPI_WARPS);   // the MMA thread and every epilogue warp
         }
-        sm100::mbar_init(mma_done, 1);
-        for (int s = 0; s < 4; ++s) sm100::mbar_init(&tau_ready[s], qps);   // the slot's quarters' writers
-        *abort_flag = 0;
+        for (int b = 0; b < T::NBUF; ++b) {
+            sm100::mbar_init(&sh.acc_full[b], 1);
+            sm100::mbar_init(&sh.acc_empty[b], PARTS * QPS);       // the slot's epilogue warps
+        }
+        sm100::mbar_init(sh.mma_done, 1);
+        for (int s = 0; s < 4; ++s) sm100::mbar_init(&sh.tau_ready[s], QPS);   // the slot's quarters' writers
+        *sh.abort_flag = 0;
         sm100::fence_mbar_init();
     }
-    if (warp == 1) sm100::tmem_alloc(tmem_slot, TMEM_COLS);
+    if (warp == 1) sm100::tmem_alloc(sh.tmem_slot, TMEM_COLS);
     sm100::tc_fence_before();
     __syncthreads();
     sm100::tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
+    const uint32_t tmem = *sh.tmem_slot;
 
     if (warp == 0) {
-        if (lane == 0) {
-            if constexpr (BN == 256) {                // one or two slots
-                if (nslot == 1) produce<BN, 1>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
-                else produce<BN, 2>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
-            } else {
-                if (nslot == 1) produce<BN, 1>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
-                else if (nslot == 2) produce<BN, 2>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
-                else produce<BN, 4>(tmQ, tmC, p, it, nt, sA, sB, full, empty, a_full, abort_flag);
-            }
-        }
+        if (lane == 0) produce<BN, NS>(tmQ, tmC, p, items, n_items, queue, sh);
+        __syncwarp();
     } else if (warp == 1) {
-        if (lane == 0) {
-            if constexpr (BN == 256) {
-                if (nslot == 1)
-                    issue<BN, 1, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready, mma_done,
-                                      abort_flag);
-                else
-                    issue<BN, 2, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready, mma_done,
-                                      abort_flag);
-            } else {
-                if (nslot == 1)
-                    issue<BN, 1, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready,
-                                           mma_done, abort_flag);
-                else if (nslot == 2)
-                    issue<BN, 2, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready,
-                                           mma_done, abort_flag);
-                else
-                    issue<BN, 4, FP8, TAU>(nt, nk, tmem, sA, sB, full, empty, a_full, acc_full, acc_empty, tau_ready,
-                                           mma_done, abort_flag);
-            }
-        }
+        if (lane == 0) issue<BN, NS, FP8, TAU>(p, items, nk, tmem, sh);
         __syncwarp();
     } else {
-        epilogue<BN, TAU>(p, it, nt, qps, bps, tau_rank(FP8), tmem, sA, tau_k, lists, sTau, sCnt, acc_full, acc_empty, tau_ready, abort_flag,
-                     lo, scratch, warp, lane);
+        epilogue<BN, NS, TAU>(p, items, tau_rank(FP8), tmem, tau_k, sh, lo, scratch, warp, lane);
     }
     sm100::tc_fence_before();
     __syncthreads();
@@ -923,7 +1011,7 @@ k_knn_tc(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtens
         sm100::tc_fence_after();
         sm100::tmem_dealloc(tmem, TMEM_COLS);
     }
-    if (threadIdx.x == 0 && *abort_flag) atomicExch(scratch + irc::kScratchErr, 1);
+    if (threadIdx.x == 0 && *sh.abort_flag) atomicExch(scratch + irc::kScratchErr, 1);
 }
 
 // Exact re-rank kernel: one warp per query of the plan, in query order (the
@@ -979,16 +1067,21 @@ static cudaEvent_t *profile_slot()
     return &g_prof_ev[3 * g_prof_used++];
 }
 
-template <bool FP8, int BN, bool TAU>
+template <bool FP8, int BN, bool TAU, int NS>
 static int launch_filter(const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const irc_tc::TcItem *items,
-                         int n_items, int nk, int tau_k, const ListOut &lo, cudaStream_t s)
+                         int n_items, unsigned *queue, int nk, int tau_k, const ListOut &lo, cudaStream_t s)
 {
     if (n_items <= 0) return IRC_OK;
-    auto kern = k_knn_tc<FP8, BN, TAU>;
+    auto kern = k_knn_tc<FP8, BN, TAU, NS>;
     const int smem = (int)Tile<BN>::SMEM_BYTES;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): smem attribute");
-    kern<<<n_items, THREADS, smem, s>>>(mq, mc, pl->dev, items, nk, tau_k, lo, pl->scratch);
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, pl->device);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): launch attributes");
+    // persistent: one CTA per SM (shared memory and TMEM allow one), each
+    // taking items from the queue until it is empty
+    const int grid = n_items < sms ? n_items : sms;
+    kern<<<grid, THREADS, smem, s>>>(mq, mc, pl->dev, items, n_items, queue, nk, tau_k, lo, pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core)");
     return IRC_OK;
 }
@@ -999,7 +1092,7 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
 {
     const int n_out = pl->dev.n_out;
     cudaError_t e = cudaMemsetAsync(lo.qinfo, 0xff, (size_t)n_out * sizeof(int2), s);   // (-1, -1): no list
-    if (e == cudaSuccess) e = cudaMemsetAsync(lo.count, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(lo.count, 0, 4 * sizeof(unsigned), s);     // count, queue heads
     if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_site_knn(tensor core): memset");
     // BF16: the pass-2 thresholds go into K positions nC + 6 .. nC + 8 of the
     // query rows when they fit (else, and for FP8, pass 2 compares in the
@@ -1010,21 +1103,26 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
     const int nk = (used + 31) / 32;
     cudaEvent_t *ev = profile_slot();
     if (ev) cudaEventRecord(ev[0], s);
-    // items of one or two slots on 256-candidate units, then four-slot items on 128
-    const int nw = pl->n_tc_wide, nn = pl->n_tc_items - pl->n_tc_wide;
-    // Four-slot items (small chunks) keep the compare in the epilogue: their
-    // CTAs are short, and waiting for the thresholds before the pass-2 MMAs
-    // would put the threshold step on their critical path.  The width never
-    // changes the results.
+    // one persistent launch per packing class: one-slot and two-slot items on
+    // 256-candidate units, then four-slot items on 128.  Four-slot items
+    // (small chunks) keep the compare in the epilogue: their CTAs are short,
+    // and waiting for the thresholds before the pass-2 MMAs would put the
+    // threshold step on their critical path.  The width never changes the
+    // results.
+    const int n1 = pl->n_tc_one, n2 = pl->n_tc_wide - pl->n_tc_one, n4 = pl->n_tc_items - pl->n_tc_wide;
+    const irc_tc::TcItem *it1 = pl->tc_items, *it2 = it1 + n1, *it4 = it2 + n2;
     using yes = std::true_type;
     using no = std::false_type;
     auto run = [&](auto tau_c) {
         constexpr bool T = decltype(tau_c)::value;
-        int r = fp8 ? launch_filter<true, 256, false>(mq, mc, pl, pl->tc_items, nw, nk, tau_k, lo, s)
-                    : launch_filter<false, 256, T>(mq, mc, pl, pl->tc_items, nw, nk, tau_k, lo, s);
+        int r = fp8 ? launch_filter<true, 256, false, 1>(mq, mc, pl, it1, n1, lo.count + 1, nk, tau_k, lo, s)
+                    : launch_filter<false, 256, T, 1>(mq, mc, pl, it1, n1, lo.count + 1, nk, tau_k, lo, s);
         if (r != IRC_OK) return r;
-        return fp8 ? launch_filter<true, 128, false>(mq, mc, pl, pl->tc_items + nw, nn, nk, tau_k, lo, s)
-                   : launch_filter<false, 128, false>(mq, mc, pl, pl->tc_items + nw, nn, nk, tau_k, lo, s);
+        r = fp8 ? launch_filter<true, 256, false, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s)
+                : launch_filter<false, 256, T, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s);
+        if (r != IRC_OK) return r;
+        return fp8 ? launch_filter<true, 128, false, 4>(mq, mc, pl, it4, n4, lo.count + 3, nk, tau_k, lo, s)
+                   : launch_filter<false, 128, false, 4>(mq, mc, pl, it4, n4, lo.count + 3, nk, tau_k, lo, s);
     };
     const int rc = tau_k >= 0 ? run(yes{}) : run(no{});
     if (rc != IRC_OK) return rc;

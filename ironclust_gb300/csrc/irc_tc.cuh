@@ -24,8 +24,8 @@ inline __host__ __device__ int fp_row4(int nC) { return 2 * ((nC + 7) / 8); }
 struct ListOut {
     int2 *qinfo;
     uint32_t *lists;
-    unsigned *count;
-    unsigned cap;
+    unsigned *count;             // count[0]: list entries used; count[1..3]: work-queue heads of the
+    unsigned cap;                // filter's one-, two- and four-slot launches
 };
 
 // Entries of the list area of a plan with n_out queries (offsets are int32).
@@ -35,7 +35,8 @@ inline size_t list_cap(long long n_out)
     return c < m ? c : m;
 }
 
-// Bytes of the list area of a plan with n_out queries (qinfo, count, lists).
+// Bytes of the list area of a plan with n_out queries (qinfo, the count and
+// the filter's three work-queue counters in one 256-byte block, lists).
 inline size_t list_area_bytes(long long n_out)
 {
     return (((size_t)n_out * 8 + 255) & ~(size_t)255) + 256 + list_cap(n_out) * 4;
@@ -53,9 +54,9 @@ inline ListOut list_area(void *base, long long n_out)
     return lo;
 }
 
-// The filter (items of one or two slots on 256-candidate units, four-slot
-// items on 128-candidate units; mc is the candidate-row map with 128-row
-// boxes) and the re-rank, on stream s.
+// The filter (one persistent launch per packing class: items of one or two
+// slots on 256-candidate units, four-slot items on 128-candidate units; mc is
+// the candidate-row map with 128-row boxes) and the re-rank, on stream s.
 int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_plan *pl, const float *F,
                   const float4 *Fp, int nC, int knn, float *vrKnn, float *rho, int32_t *miKnn, float *d2Knn,
                   const ListOut &lo, cudaStream_t s);
