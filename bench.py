@@ -158,8 +158,8 @@ def run_ours(args):
     for mode in forms:
         if mode in ("bf16", "fp8"):
             t = autotune.tune(P, F, KNN, mode, use_cache=False)
-            tuned[mode] = {"layout": {"max_slots": t["layout"][0], "order": t["layout"][1]},
-                           "knn_ms": {"%d,%d" % k: v for k, v in t["ms"].items()}}
+            tuned[mode] = {"layout": {"max_slots": t["layout"][0], "order": t["layout"][1], "unit_width": t["layout"][2]},
+                           "knn_ms": {",".join(map(str, k)): v for k, v in t["ms"].items()}}
 
         def step():
             return irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
@@ -431,8 +431,8 @@ def run_batched(args, dev, torch, irc, flush, stream, dist=None):
         tuned = None
         if mode in ("bf16", "fp8"):
             t = autotune.tune(P, F, KNN, mode, use_cache=False)
-            tuned = {"layout": {"max_slots": t["layout"][0], "order": t["layout"][1]},
-                     "knn_ms": {"%d,%d" % k: v for k, v in t["ms"].items()}}
+            tuned = {"layout": {"max_slots": t["layout"][0], "order": t["layout"][1], "unit_width": t["layout"][2]},
+                     "knn_ms": {",".join(map(str, k)): v for k, v in t["ms"].items()}}
         for _ in range(2):
             irc.knn_rho_delta_site(P, F, knn=KNN, mode=mode)
         torch.cuda.synchronize()

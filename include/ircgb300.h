@@ -201,6 +201,15 @@ int irc_plan_check(irc_plan *plan, void *stream);
  * call it outside stream capture.  No reference counterpart. */
 int irc_plan_tc_layout(irc_plan *plan, int max_slots, int order);
 
+/* Candidate-unit width of the plan's one- and two-slot tensor-core work items
+ * (IRC_MODE_BF16 / FP8): 256 (default: one N = 256 MMA per K slice, two
+ * 256-column accumulators, the threshold folded into the MMA for BF16) or 128
+ * (N = 128, four 128-column accumulators, the threshold compared in the
+ * epilogue).  Four-slot items always use 128.  Results do not depend on it,
+ * only speed does (ironclust_gb300.autotune picks it with the layout).  No
+ * reference counterpart. */
+int irc_plan_tc_units(irc_plan *plan, int width);
+
 /* Working memory of the tensor-core modes: bytes a plan needs for nC
  * features (operand rows of all nF columns + their padded FP32 copy).  By
  * default a plan allocates it on its first tensor-core call and keeps it;

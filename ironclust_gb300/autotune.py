@@ -1,13 +1,15 @@
-"""Autotuner of the tensor-core kNN's work layout.
+"""Autotuner of the tensor-core kNN's work layout and tile shape.
 
-The tensor-core kNN (irc_site_knn in IRC_MODE_BF16 / FP8) runs one CTA per
-work item: 128 queries of a large chunk, or the remainders of up to
-max_slots small chunks packed side by side (irc_plan_tc_layout).  Which
-packing and item order is fastest depends on the feature dimension and on
-the chunk sizes (a probe-scale batch has thousands of ~20-query chunks, a
-single drift site a few hundred 2,000-query chunks), so it is measured, not
-guessed: every candidate layout is timed on the plan itself with CUDA events
-and the fastest is applied.  Results do not depend on the layout.
+The tensor-core kNN (irc_site_knn in IRC_MODE_BF16 / FP8) serves work items:
+128 queries of a large chunk, or the remainders of up to max_slots small
+chunks packed side by side (irc_plan_tc_layout), each item's candidates
+streamed in units of 256 or 128 candidates (irc_plan_tc_units: the MMA width
+N of the one- and two-slot items, with two or four accumulators in TMEM).
+Which packing, item order and unit width are fastest depends on the feature
+dimension and on the chunk sizes (a probe-scale batch has thousands of
+~20-query chunks, a single drift site a few hundred 2,000-query chunks), so
+they are measured, not guessed: every candidate is timed on the plan itself
+with CUDA events and the fastest is applied.  Results depend on none of them.
 
 Decisions are cached per (device, form, feature dimension, chunk-size and
 candidate-count buckets) in a JSON file ($IRC_TUNE_CACHE, default
@@ -26,8 +28,9 @@ import torch
 from . import irc
 from ._lib import check, lib
 
-# (max_slots, order): the layouts tried, the default first
-CANDIDATES = [(4, 0), (2, 0), (1, 0), (4, 1)]
+# (max_slots, order, unit width): the candidates tried, the default first
+CANDIDATES = [(4, 0, 256), (2, 0, 256), (1, 0, 256), (4, 1, 256), (4, 0, 128), (2, 0, 128), (1, 0, 128),
+              (4, 1, 128)]
 
 
 def cache_path():
@@ -71,7 +74,10 @@ def _store(table):
 
 
 def apply(plan, layout):
+    """layout: (max_slots, order[, unit width]) -- a width left out is 256."""
     check(lib().irc_plan_tc_layout(plan.h, int(layout[0]), int(layout[1])), "irc_plan_tc_layout")
+    width = int(layout[2]) if len(layout) > 2 else 256
+    check(lib().irc_plan_tc_units(plan.h, width), "irc_plan_tc_units")
 
 
 def time_layout(plan, F, layout, knn=30, mode="bf16", reps=2):
@@ -92,12 +98,13 @@ def time_layout(plan, F, layout, knn=30, mode="bf16", reps=2):
 
 def tune(plan, F, knn=30, mode="bf16", reps=2, use_cache=True, candidates=None):
     """Pick and apply the fastest layout for this plan.  Returns
-    dict(layout=(max_slots, order), ms={layout: ms} (empty when cached),
-    key, cached)."""
+    dict(layout=(max_slots, order, unit width), ms={layout: ms} (empty when
+    cached), key, cached)."""
     key = signature(plan, F.shape[1], mode)
     table = _load() if use_cache else {}
     if key in table:
         layout = tuple(table[key]["layout"])
+        layout = layout + (256,) * (3 - len(layout))          # entries written before the width was tuned
         apply(plan, layout)
         return dict(layout=layout, ms={}, key=key, cached=True)
     times = {}
@@ -107,6 +114,6 @@ def tune(plan, F, knn=30, mode="bf16", reps=2, use_cache=True, candidates=None):
     apply(plan, best)
     if use_cache:
         table = _load()
-        table[key] = dict(layout=list(best), ms={"%d,%d" % k: v for k, v in times.items()})
+        table[key] = dict(layout=list(best), ms={",".join(map(str, k)): v for k, v in times.items()})
         _store(table)
     return dict(layout=best, ms=times, key=key, cached=False)

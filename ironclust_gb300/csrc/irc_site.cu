@@ -575,6 +575,16 @@ int irc_plan_tc_layout(irc_plan *pl, int max_slots, int order)
     return IRC_OK;
 }
 
+int irc_plan_tc_units(irc_plan *pl, int width)
+{
+    if (!pl || (width != 128 && width != 256)) {
+        irc_host::set_error("irc_plan_tc_units: need a plan and a width of 128 or 256");
+        return IRC_E_INVAL;
+    }
+    pl->tc_wide_bn = width;
+    return IRC_OK;
+}
+
 int irc_plan_check(irc_plan *pl, void *stream)
 {
     if (!pl) { irc_host::set_error("irc_plan_check: null plan"); return IRC_E_INVAL; }

@@ -1104,22 +1104,33 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
     cudaEvent_t *ev = profile_slot();
     if (ev) cudaEventRecord(ev[0], s);
     // one persistent launch per packing class: one-slot and two-slot items on
-    // 256-candidate units, then four-slot items on 128.  Four-slot items
-    // (small chunks) keep the compare in the epilogue: their CTAs are short,
-    // and waiting for the thresholds before the pass-2 MMAs would put the
-    // threshold step on their critical path.  The width never changes the
-    // results.
+    // 256-candidate units (or 128, irc_plan_tc_units), then four-slot items
+    // on 128.  The threshold goes into the MMA only on 256-wide units; the
+    // narrower ones compare in the epilogue.  Four-slot items (small chunks)
+    // keep the compare: their CTAs are short, and waiting for the thresholds
+    // before the pass-2 MMAs would put the threshold step on their critical
+    // path.  Neither the width nor the packing changes the results.
     const int n1 = pl->n_tc_one, n2 = pl->n_tc_wide - pl->n_tc_one, n4 = pl->n_tc_items - pl->n_tc_wide;
     const irc_tc::TcItem *it1 = pl->tc_items, *it2 = it1 + n1, *it4 = it2 + n2;
+    const bool narrow = pl->tc_wide_bn == 128;
     using yes = std::true_type;
     using no = std::false_type;
     auto run = [&](auto tau_c) {
         constexpr bool T = decltype(tau_c)::value;
-        int r = fp8 ? launch_filter<true, 256, false, 1>(mq, mc, pl, it1, n1, lo.count + 1, nk, tau_k, lo, s)
+        int r;
+        if (narrow)
+            r = fp8 ? launch_filter<true, 128, false, 1>(mq, mc, pl, it1, n1, lo.count + 1, nk, tau_k, lo, s)
+                    : launch_filter<false, 128, false, 1>(mq, mc, pl, it1, n1, lo.count + 1, nk, tau_k, lo, s);
+        else
+            r = fp8 ? launch_filter<true, 256, false, 1>(mq, mc, pl, it1, n1, lo.count + 1, nk, tau_k, lo, s)
                     : launch_filter<false, 256, T, 1>(mq, mc, pl, it1, n1, lo.count + 1, nk, tau_k, lo, s);
         if (r != IRC_OK) return r;
-        r = fp8 ? launch_filter<true, 256, false, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s)
-                : launch_filter<false, 256, T, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s);
+        if (narrow)
+            r = fp8 ? launch_filter<true, 128, false, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s)
+                    : launch_filter<false, 128, false, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s);
+        else
+            r = fp8 ? launch_filter<true, 256, false, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s)
+                    : launch_filter<false, 256, T, 2>(mq, mc, pl, it2, n2, lo.count + 2, nk, tau_k, lo, s);
         if (r != IRC_OK) return r;
         return fp8 ? launch_filter<true, 128, false, 4>(mq, mc, pl, it4, n4, lo.count + 3, nk, tau_k, lo, s)
                    : launch_filter<false, 128, false, 4>(mq, mc, pl, it4, n4, lo.count + 3, nk, tau_k, lo, s);
