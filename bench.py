@@ -374,7 +374,7 @@ def run_batched(args, dev, torch, irc, flush, stream, dist=None):
     else:
         mine, work = list(range(b.n_sites)), b
     F = torch.from_numpy(work.F).to(dev)
-    P = irc.Plan(work.plan)
+    P = work.make_plan()
     res = {"workload": "probe10m" if args.probe_sites == 384 else "probe%d" % args.probe_sites,
            "sites": b.n_sites, "spikes": N, "chunks": int(len(b.plan["q0"])), "pairs": plan_pairs(b.plan),
            "dims": sorted(set(int(d) for d in b.dims)), "generation_s": gen_s, "forms": {}}
@@ -456,7 +456,7 @@ def run_batched(args, dev, torch, irc, flush, stream, dist=None):
             host = {k: out[k].cpu().numpy() for k in keys}
             merged = shard.gather_merge(b, mine, host, rank, world, cpu_group)
             if rank == 0:
-                Pw, Fw = irc.Plan(b.plan), torch.from_numpy(b.F).to(dev)
+                Pw, Fw = b.make_plan(), torch.from_numpy(b.F).to(dev)
                 whole = irc.knn_rho_delta_site(Pw, Fw, knn=KNN, mode=mode)
                 same = all(np.array_equal(merged[k].view(np.int32), whole[k].cpu().numpy().view(np.int32))
                            for k in keys)

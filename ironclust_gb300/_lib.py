@@ -42,6 +42,7 @@ SIGNATURES = {
     "irc_plan_check": [_P, _P],
     "irc_plan_tc_layout": [_P, _I, _I],
     "irc_plan_tc_units": [_P, _I],
+    "irc_plan_set_site_dims": [_P, _I, _P, _P],
     "irc_plan_tc_bytes": [_P, _I],
     "irc_plan_set_tc_buffer": [_P, _P, C.c_size_t],
     "irc_knn_rho_delta_site": [_P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P],

@@ -67,6 +67,13 @@ class SiteBatch:
         """kNN rows of site i with indices local to that site (1-based)."""
         return np.asarray(miKnn)[self.site_slice(i)] - int(self.bases[i])
 
+    def make_plan(self):
+        """irc.Plan of the batch with its site widths set
+        (irc_plan_set_site_dims): the tensor-core re-rank skips each site's
+        padded features."""
+        from . import irc
+        return irc.Plan(self.plan).set_site_dims(self.bases, self.dims)
+
     def c_plan(self):
         """The batch plan built by the library from the per-site plans
         (irc_batch_plan_create), the route of a C or MATLAB host."""
@@ -81,7 +88,7 @@ class SiteBatch:
         h = C.c_void_p()
         check(lib().irc_batch_plan_create(C.byref(h), self.n_sites, *[a.ctypes.data_as(C.c_void_p) for a in arrs]),
               "irc_batch_plan_create")
-        return irc.Plan.from_handle(h, self.plan)
+        return irc.Plan.from_handle(h, self.plan).set_site_dims(self.bases, self.dims)
 
     def stack_device(self, F_sites):
         """The stacked feature matrix from per-site device tensors

@@ -77,6 +77,7 @@ struct irc_plan {
     int n_tc_one;                          // items [0, n_tc_one) have one slot, [n_tc_one, n_tc_wide) two
     int n_tc_wide;                         // (both on 256-candidate units), the rest four (128-candidate units)
     int tc_wide_bn;                        // unit width of the one- and two-slot items: 256 (0 = default) or 128
+    uint8_t *row_dims;                     // [nF] features of each row's site (irc_plan_set_site_dims) or null
     void *tc_items_buf;                    // items of irc_plan_tc_layout, when called
     void *tc_buf;                          // tensor-core operand rows (2 x nF x tc_row_bytes) and the
                                            // padded FP32 rows of the re-rank, allocated lazily

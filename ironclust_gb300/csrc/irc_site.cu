@@ -519,6 +519,7 @@ int irc_plan_destroy(irc_plan *pl)
     cudaError_t e = cudaFree(pl->dmem);
     if (pl->tc_buf && !pl->tc_external) cudaFree(pl->tc_buf);
     if (pl->tc_items_buf) cudaFree(pl->tc_items_buf);
+    if (pl->row_dims) cudaFree(pl->row_dims);
     free(pl->h_q0); free(pl->h_nq); free(pl->h_roff); free(pl->h_rs); free(pl->h_rn);
     free(pl);
     return e == cudaSuccess ? IRC_OK : irc_host::cuda_status(e, "irc_plan_destroy");
@@ -572,6 +573,52 @@ int irc_plan_tc_layout(irc_plan *pl, int max_slots, int order)
     pl->n_tc_items = (int)items.size();
     pl->n_tc_one = n_one;
     pl->n_tc_wide = n_wide;
+    return IRC_OK;
+}
+
+int irc_plan_set_site_dims(irc_plan *pl, int nSites, const int64_t *row_base, const int32_t *dims)
+{
+    if (!pl) { irc_host::set_error("irc_plan_set_site_dims: null plan"); return IRC_E_INVAL; }
+    if (nSites == 0) {                            // clear
+        if (pl->row_dims) cudaFree(pl->row_dims);
+        pl->row_dims = nullptr;
+        return IRC_OK;
+    }
+    const int nF = pl->dev.nF;
+    if (nSites < 0 || !row_base || !dims || row_base[0] != 0 || row_base[nSites] != nF) {
+        irc_host::set_error("irc_plan_set_site_dims: need row_base[0] = 0 and row_base[nSites] = nF (%d)", nF);
+        return IRC_E_INVAL;
+    }
+    for (int k = 0; k < nSites; ++k)
+        if (row_base[k + 1] < row_base[k] || dims[k] < 1 || dims[k] > IRC_NC_MAX) {
+            irc_host::set_error("irc_plan_set_site_dims: site %d: bad rows or dims", k);
+            return IRC_E_INVAL;
+        }
+    // every chunk's queries and candidate runs lie in one site (the site of
+    // its first query): the site's width then bounds every distance it needs
+    auto site_of = [&](long long r) {
+        return (int)(std::upper_bound(row_base, row_base + nSites + 1, (int64_t)r) - row_base) - 1;
+    };
+    for (int i = 0; i < pl->dev.nChunks; ++i) {
+        if (pl->h_nq[i] <= 0) continue;
+        const int st = site_of(pl->h_q0[i]);
+        bool ok = site_of((long long)pl->h_q0[i] + pl->h_nq[i] - 1) == st;
+        for (int r = pl->h_roff[i]; ok && r < pl->h_roff[i + 1]; ++r)
+            ok = pl->h_rn[r] <= 0 || (site_of(pl->h_rs[r]) == st && site_of((long long)pl->h_rs[r] + pl->h_rn[r] - 1) == st);
+        if (!ok) {
+            irc_host::set_error("irc_plan_set_site_dims: chunk %d reaches outside the site of its queries", i);
+            return IRC_E_INVAL;
+        }
+    }
+    std::vector<uint8_t> h((size_t)nF);
+    for (int k = 0; k < nSites; ++k)
+        for (long long r = row_base[k]; r < row_base[k + 1]; ++r) h[(size_t)r] = (uint8_t)dims[k];
+    if (!pl->row_dims) {
+        cudaError_t e = cudaMalloc(&pl->row_dims, h.size() ? h.size() : 1);
+        if (e != cudaSuccess) { pl->row_dims = nullptr; return irc_host::cuda_status(e, "irc_plan_set_site_dims"); }
+    }
+    cudaError_t e = cudaMemcpy(pl->row_dims, h.data(), h.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return irc_host::cuda_status(e, "irc_plan_set_site_dims: upload");
     return IRC_OK;
 }
 

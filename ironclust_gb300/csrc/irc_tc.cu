@@ -180,10 +180,10 @@ __device__ __forceinline__ void warp_bitonic(T (&v)[PER], int lane)
     }
 }
 
-__device__ __forceinline__ double dist2_f64(const float *__restrict__ b, const float *__restrict__ a, int nC)
+__device__ __forceinline__ double dist2_f64(const float *__restrict__ b, const float *__restrict__ a, int nd)
 {
     double acc = 0.0;
-    for (int c = 0; c < nC; ++c) {
+    for (int c = 0; c < nd; ++c) {
         const double d = (double)__ldg(b + c) - (double)__ldg(a + c);
         acc = __dadd_rn(acc, __dmul_rn(d, d));
     }
@@ -217,13 +217,16 @@ __device__ __forceinline__ void ld_nc_v8(const float *p, float (&v)[8])
 
 // Exact re-rank of the cL candidates listed for query q (list[0 .. cL)),
 // warp-cooperative; o = q - q_base.  Requires knn <= 32.  Candidate e is
-// lane e % 32 of round e / 32, and every lane gathers its own rows.
+// lane e % 32 of round e / 32, and every lane gathers its own rows.  nC is
+// the row stride of F; nd <= nC the features that can be non-zero for this
+// query and its candidates (the width of their site): the rest are zero in
+// both rows and add exactly 0 to every distance, so they are skipped.
 template <int PER>
 __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL, bool complete, int q,
                                        const float *__restrict__ F, const float4 *__restrict__ Fp, int Dp4,
-                                       float4 *__restrict__ qs, int nC, int knn, size_t o, unsigned long long *ws,
-                                       int lane, int margin, int *miKnn, float *d2Knn, float *vrKnn, float *rho,
-                                       int *scratch)
+                                       float4 *__restrict__ qs, int nC, int nd, int knn, size_t o,
+                                       unsigned long long *ws, int lane, int margin, int *miKnn, float *d2Knn,
+                                       float *vrKnn, float *rho, int *scratch)
 {
     const float *a = F + (size_t)q * nC;
     // the query row, staged once per warp (broadcast reads below)
@@ -245,7 +248,7 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
             const float *bs = reinterpret_cast<const float *>(Fp + (size_t)idx * Dp4);
             float acc = 0.0f;
 #pragma unroll 2
-            for (int c8 = 0; c8 < Dp4 / 2; ++c8) {
+            for (int c8 = 0; c8 < (nd + 7) / 8; ++c8) {
                 float bv[8];
                 ld_nc_v8(bs + 8 * c8, bv);
                 const float4 a0 = qs[2 * c8], a1 = qs[2 * c8 + 1];
@@ -254,7 +257,7 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
                 acc = irc::dterm(acc, bv[0], av[0]);
 #pragma unroll
                 for (int u = 1; u < 8; ++u)
-                    if (c + u < nC) acc = irc::dterm(acc, bv[u], av[u]);
+                    if (c + u < nd) acc = irc::dterm(acc, bv[u], av[u]);
             }
             if (acc > 0.0f && acc < IRC_SINGLE_INF_F)
                 kv[bi] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
@@ -349,7 +352,7 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
         // lanes j < nb hold band element lo + j; rank them by (FP64 distance, index)
         const unsigned long long kb = lane < nb ? ws[lo + lane] : ~0ull;
         const int ib = (int)(kb & 0xffffffffu);
-        const double db = lane < nb ? dist2_f64(F + (size_t)ib * nC, a, nC) : 0.0;
+        const double db = lane < nb ? dist2_f64(F + (size_t)ib * nC, a, nd) : 0.0;
         int rank = 0;
         for (int m = 0; m < nb; ++m) {
             const double dm = __shfl_sync(0xffffffffu, db, m);
@@ -1022,8 +1025,9 @@ constexpr int RR_WARPS = 8;
 
 __global__ void __launch_bounds__(32 * RR_WARPS, 4)
 k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int n_out, int q_base,
-         const float *__restrict__ F, const float4 *__restrict__ Fp, int nC, int knn, float *__restrict__ vrKnn,
-         float *__restrict__ rho, int *__restrict__ miKnn, float *__restrict__ d2Knn, int margin, int *__restrict__ scratch)
+         const float *__restrict__ F, const float4 *__restrict__ Fp, int nC, const uint8_t *__restrict__ row_dims,
+         int knn, float *__restrict__ vrKnn, float *__restrict__ rho, int *__restrict__ miKnn,
+         float *__restrict__ d2Knn, int margin, int *__restrict__ scratch)
 {
     __shared__ unsigned long long wkeys[RR_WARPS * WARP_KEYS];
     __shared__ float4 qrows[RR_WARPS * QROW4];
@@ -1035,17 +1039,18 @@ k_rerank(const int2 *__restrict__ qinfo, const uint32_t *__restrict__ lists, int
     const int Dp4 = irc_tc::fp_row4(nC);
     const uint32_t *lst = lists + (unsigned)qi.x;
     const int cL = qi.y & 0x3fffffff, q = q_base + o;
+    const int nd = row_dims ? min(nC, (int)__ldg(row_dims + q)) : nC;
     const bool complete = (qi.y >> 30) & 1;
     unsigned long long *ws = wkeys + warp * WARP_KEYS;
     float4 *qs = qrows + warp * QROW4;
     if (cL <= 64)
-        rerank<2>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
+        rerank<2>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, nd, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
                   scratch);
     else if (cL <= 128)
-        rerank<4>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
+        rerank<4>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, nd, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
                   scratch);
     else
-        rerank<8>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
+        rerank<8>(lst, cL, complete, q, F, Fp, Dp4, qs, nC, nd, knn, (size_t)o, ws, lane, margin, miKnn, d2Knn, vrKnn, rho,
                   scratch);
 }
 
@@ -1139,8 +1144,8 @@ int launch_knn_tc(bool fp8, const CUtensorMap &mq, const CUtensorMap &mc, irc_pl
     if (rc != IRC_OK) return rc;
     if (ev) cudaEventRecord(ev[1], s);
     k_rerank<<<(n_out + RR_WARPS - 1) / RR_WARPS, 32 * RR_WARPS, 0, s>>>(
-        lo.qinfo, lo.lists, n_out, pl->dev.q_base, F, Fp, nC, knn, vrKnn, rho, miKnn, d2Knn, crowd_margin(fp8),
-        pl->scratch);
+        lo.qinfo, lo.lists, n_out, pl->dev.q_base, F, Fp, nC, pl->row_dims, knn, vrKnn, rho, miKnn, d2Knn,
+        crowd_margin(fp8), pl->scratch);
     IRC_CHECK_LAUNCH("irc_site_knn(tensor core) re-rank");
     if (ev) cudaEventRecord(ev[2], s);
     return IRC_OK;

@@ -297,6 +297,15 @@ class Plan:
     def n_out(self):
         return int(self.d["n_out"])
 
+    def set_site_dims(self, row_base, dims):
+        """irc_plan_set_site_dims: rows row_base[k] .. row_base[k+1]-1 form
+        site k, whose features past dims[k] are zero (a stacked batch)."""
+        rb = np.ascontiguousarray(row_base, np.int64)
+        dd = np.ascontiguousarray(dims, np.int32)
+        check(lib().irc_plan_set_site_dims(self.h, len(dd), rb.ctypes.data_as(C.c_void_p),
+                                           dd.ctypes.data_as(C.c_void_p)), "irc_plan_set_site_dims")
+        return self
+
     def close(self):
         if self.h:
             lib().irc_plan_destroy(self.h)

@@ -123,3 +123,35 @@ def test_c_batch_plan_rejects_a_run_leaving_its_site(gpu, sites):
     h = C.c_void_p()
     rc = _lib.lib().irc_batch_plan_create(C.byref(h), 2, *[a.ctypes.data_as(C.c_void_p) for a in arrs])
     assert rc != 0 and not h.value
+
+
+@pytest.mark.parametrize("mode", ["bf16", "fp8"])
+def test_site_dims_skip_padding_with_identical_results(gpu, sites, mode):
+    """irc_plan_set_site_dims: the re-rank stops at each site's own width;
+    the padded features are zero in both rows, so every output is the same
+    bit for bit as without the widths."""
+    b = batch.SiteBatch(sites)
+    F = torch.from_numpy(b.F).to(gpu)
+    P0, P1 = irc.Plan(b.plan), b.make_plan()
+    r0 = irc.knn_rho_delta_site(P0, F, knn=30, mode=mode)
+    r1 = irc.knn_rho_delta_site(P1, F, knn=30, mode=mode)
+    for k in ("miKnn", "nneigh"):
+        assert np.array_equal(r0[k].cpu().numpy(), r1[k].cpu().numpy()), k
+    for k in ("rho", "delta", "d2Knn"):
+        assert np.array_equal(r0[k].cpu().numpy().view(np.int32), r1[k].cpu().numpy().view(np.int32)), k
+    P1.set_site_dims(np.zeros(1, np.int64), np.zeros(0, np.int32))       # nSites = 0 clears
+    r2 = irc.knn_rho_delta_site(P1, F, knn=30, mode=mode)
+    assert np.array_equal(r2["miKnn"].cpu().numpy(), r0["miKnn"].cpu().numpy())
+
+
+def test_site_dims_reject_a_chunk_outside_its_site(gpu, sites):
+    from ironclust_gb300 import _lib
+    b = batch.SiteBatch(sites[:2])
+    P = irc.Plan(b.plan)
+    with pytest.raises(_lib.IrcError):                                   # sites split inside a chunk
+        P.set_site_dims(np.array([0, 7, b.F.shape[0]], np.int64), np.array([18, 33], np.int32))
+    with pytest.raises(_lib.IrcError):                                   # rows not covering nF
+        P.set_site_dims(np.array([0, 10], np.int64), np.array([18], np.int32))
+    with pytest.raises(_lib.IrcError):                                   # width out of range
+        P.set_site_dims(np.ascontiguousarray(b.bases, np.int64), np.array([18, 99], np.int32))
+    P.set_site_dims(b.bases, b.dims)
