@@ -47,7 +47,7 @@ METRIC = "kNN+rho+delta spikes/s: BF16-TC vs FP32 form on one GB300 at >=99.9% k
 WORKLOAD = "drift400k"
 KNN = 30
 MIN_COUNT = 30          # min_count of the reference's default parameters (matlab/default.prm:120)
-TC_KNN_TRAFFIC_BYTES = 134.55e6 + 105.35e6   # ncu, one k_knn_tc launch on drift400k (read + write)
+TC_KNN_TRAFFIC_BYTES = 130.67e6 + 59.72e6    # ncu, one k_knn_tc launch on drift400k (read + write)
 
 
 def _dist_env():
