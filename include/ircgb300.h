@@ -214,9 +214,9 @@ int irc_plan_tc_units(irc_plan *plan, int width);
  * row_base[k] .. row_base[k+1]-1 of F belong to site k, whose features past
  * dims[k] are zero in every row (as irc_batch_stack writes them); row_base
  * spans the plan's nF rows, and every chunk's queries and candidates must lie
- * in one site (checked).  The tensor-core re-rank then skips each query's
- * zero features: same results, less work.  nSites = 0 clears it.  No
- * reference counterpart. */
+ * in one site (checked).  The tensor-core re-rank and the delta fallback
+ * scan then skip each query's zero features: same results, less work.
+ * nSites = 0 clears it.  No reference counterpart. */
 int irc_plan_set_site_dims(irc_plan *plan, int nSites, const int64_t *row_base, const int32_t *dims);
 
 /* Working memory of the tensor-core modes: bytes a plan needs for nC

@@ -353,8 +353,8 @@ k_delta_compact(irc::PlanDev p, const int *__restrict__ fb_flag, int *__restrict
 
 __global__ void __launch_bounds__(kThreads)
 k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restrict__ R, int nC,
-              const int *__restrict__ n_items, const int2 *__restrict__ items, const int *__restrict__ fb_list,
-              unsigned long long *__restrict__ keys)
+              const uint8_t *__restrict__ row_dims, const int *__restrict__ n_items, const int2 *__restrict__ items,
+              const int *__restrict__ fb_list, unsigned long long *__restrict__ keys)
 {
     __shared__ __align__(16) float sA[IRC_NC_MAX * kQB];
     __shared__ float sRA[kQB];
@@ -369,13 +369,16 @@ k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restri
         const int np = min(kParts, max(1, ntot / kMinPart));
         const int r0 = __ldg(p.roff + chunk), r1 = __ldg(p.roff + chunk + 1);
         const int seg = __ldg(p.q0 + chunk) - p.q_base;
+        // features that can be non-zero for this chunk's queries and candidates
+        // (their site's width, irc_plan_set_site_dims): the rest add exactly 0
+        const int nd = row_dims ? min(nC, (int)__ldg(row_dims + __ldg(p.q0 + chunk))) : nC;
         if (threadIdx.x < kQB) {
             const int q = fb_list[seg + first + min((int)threadIdx.x, n - 1)];
             sQ[threadIdx.x] = q;
             sRA[threadIdx.x] = __ldg(R + q);
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < nC * kQB; i += kThreads) {
+        for (int i = threadIdx.x; i < nd * kQB; i += kThreads) {
             const int c = i / kQB, q = i - c * kQB;
             sA[i] = __ldg(F + (size_t)sQ[q] * nC + c);
         }
@@ -397,7 +400,7 @@ k_delta_tiles(irc::PlanDev p, const float *__restrict__ F, const float *__restri
                     if (!(rb <= sRA[q])) live |= 1u << q;
                 if (!live) continue;
                 float acc[kQB];
-                dist_qb<kQB>(F + (size_t)iB * nC, nC, sA, acc);
+                dist_qb<kQB>(F + (size_t)iB * nC, nd, sA, acc);
 #pragma unroll
                 for (int q = 0; q < kQB; ++q)
                     if (((live >> q) & 1u) && acc[q] > 0.0f && acc[q] < kInfSentinel) {
@@ -497,7 +500,7 @@ int irc_site_delta_list(irc_plan *pl, const float *F, int nC, const float *R, in
     IRC_CHECK_LAUNCH("irc_site_delta list");
     k_delta_compact<<<pl->dev.nChunks, kThreads, 0, s>>>(pl->dev, la, lb, n_items, items, keys);
     IRC_CHECK_LAUNCH("irc_site_delta compact");
-    k_delta_tiles<<<kQueueBlocks, kThreads, 0, s>>>(pl->dev, F, R, nC, n_items, items, lb, keys);
+    k_delta_tiles<<<kQueueBlocks, kThreads, 0, s>>>(pl->dev, F, R, nC, pl->row_dims, n_items, items, lb, keys);
     IRC_CHECK_LAUNCH("irc_site_delta tiles");
     k_delta_finish<<<kQueueBlocks, kThreads, 0, s>>>(pl->dev, R, n_items, items, lb, keys, delta, nneigh);
     IRC_CHECK_LAUNCH("irc_site_delta finish");
