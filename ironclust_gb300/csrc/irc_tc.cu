@@ -279,15 +279,16 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
             return;
         }
     }
-    // ws[0 .. WARP_KEYS) <- the WARP_KEYS smallest keys, ascending.  With
-    // more than 64 keys, select first: a bitwise search (stopped at
-    // TAU_LOW_BIT, rounded up) bounds the k-th distance from above, and the
-    // keys at or below that bound plus 2^-16 relative -- the band below
-    // lies inside it -- are compacted into ws and sorted alone.  They are
+    // ws[0 .. WARP_KEYS) <- the smallest keys, ascending.  With more than
+    // 32 keys, select first: a bitwise search (stopped at TAU_LOW_BIT,
+    // rounded up) bounds the k-th distance from above, and the keys at or
+    // below that bound plus 2^-16 relative -- the band below lies inside it
+    // -- are compacted into ws and sorted alone, one per lane when at most 32
+    // pass (the usual case: about knn of them), else two per lane.  They are
     // the first positions of the full sort, so the result is the same; if
     // more than WARP_KEYS pass, the full sort runs.
     bool sorted = false;
-    if (PER > 2) {
+    if (PER >= 2) {
         unsigned ans = 0;
 #pragma unroll 1
         for (int b = 30; b >= TAU_LOW_BIT; --b) {
@@ -310,7 +311,14 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
             n += __popc(bal);
         }
         __syncwarp();
-        if (n <= WARP_KEYS) {
+        if (n <= 32) {                            // the common case: ~knn keys, one per lane
+            unsigned long long v1[1] = {lane < n ? ws[lane] : ~0ull};
+            __syncwarp();
+            warp_bitonic<unsigned long long, 1>(v1, lane);
+            ws[lane] = v1[0];
+            ws[32 + lane] = ~0ull;
+            sorted = true;
+        } else if (n <= WARP_KEYS) {
             unsigned long long v2[2];
 #pragma unroll
             for (int i = 0; i < 2; ++i) v2[i] = lane * 2 + i < n ? ws[lane * 2 + i] : ~0ull;
