@@ -279,8 +279,8 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
             return;
         }
     }
-    // ws[0 .. WARP_KEYS) <- the smallest keys, ascending.  With more than
-    // 32 keys, select first: a bitwise search (stopped at TAU_LOW_BIT,
+    // ws[0 .. WARP_KEYS) <- the smallest keys, ascending, selection first:
+    // a bitwise search (stopped at TAU_LOW_BIT,
     // rounded up) bounds the k-th distance from above, and the keys at or
     // below that bound plus 2^-16 relative -- the band below lies inside it
     // -- are compacted into ws and sorted alone, one per lane when at most 32
