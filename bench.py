@@ -48,6 +48,10 @@ WORKLOAD = "drift400k"
 KNN = 30
 MIN_COUNT = 30          # min_count of the reference's default parameters (matlab/default.prm:120)
 TC_KNN_TRAFFIC_BYTES = 130.67e6 + 59.72e6    # ncu, one k_knn_tc launch on drift400k (read + write)
+# ncu, the one-slot k_knn_tc launch of a middle block of the 100M-spike stream
+STREAM_FILTER_NCU = {"kernel": "k_knn_tc<0, 256, 1, 1>", "duration_ms": 0.698,
+                     "tensor_pipe_active_pct": 12.04, "dram_read_bytes": 124.71e6, "dram_write_bytes": 68.52e6,
+                     "dram_throughput_pct": 3.49, "source": "profiles/launches_stream100m.md"}
 
 
 def _dist_env():
@@ -546,6 +550,9 @@ def run_stream(args, dev, torch, irc):
     res["hbm_gbs_compulsory"] = r["bytes"] / (res["ms"] / 1e3) / 1e9
     res["tensor_tflops_algorithmic"] = r["flops"] / (res["ms"] / 1e3) / 1e12
     res["tensor_frac_algorithmic"] = res["tensor_tflops_algorithmic"] / _peaks()["bf16"]
+    # counters of one middle block's one-slot filter launch, from a separate ncu capture of the same
+    # streamed pass (never a number taken under the profiler in this run)
+    res["ncu_filter_launch"] = STREAM_FILTER_NCU
     if not args.no_accuracy:
         # accuracy against FP64 on the middle block (>= 1 M spikes of the recording): kNN recall,
         # rho and delta with nearest higher-rho neighbours (oracle.accuracy.stream_block_check)
