@@ -714,7 +714,7 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
             float *brow = qarea + lane * BROW + part * PART;
 #pragma unroll
             for (int c = 0; c < PART; ++c) brow[c] = fmaxf(bm[c], 0.0f);
-            if (part == 0) sh.sCnt[row] = 0;                 // list counts of pass 2 (ordered by the barriers below)
+            if (part == 0) sh.sCnt[row] = 0;      // list counts of pass 2 (ordered by the barriers below)
             slot_barrier(s, slot_threads);
             // The warp's 8 rows at once (independent chains): a bitwise
             // search, from the top, of the largest t with fewer than rank
