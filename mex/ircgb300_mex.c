@@ -27,7 +27,8 @@
  *            ircgb300_mex('knn_save_site',      vcFile_knn, fAppend, miKnn, viSpk_out, knn)
  *            ircgb300_mex('sort_save',          vcFile, rho, delta, nneigh, ordrho)
  *   [vrKnn, rho, miKnn, delta, nneigh] =
- *            ircgb300_mex('knn_rho_delta_site', F, q0, nq, roff, rs, rn, q_base, n_out, knn, mode [, R])
+ *            ircgb300_mex('knn_rho_delta_site', F, q0, nq, roff, rs, rn, q_base, n_out, knn, mode
+ *                         [, R [, site_rows, site_dims]])
  *   v      = ircgb300_mex('version')
  *
  * sort_rho replaces `vrRho = vrRho / max(vrRho); [~, ordrho] = sort(vrRho,
@@ -352,7 +353,9 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         return;
     }
     if (!strcmp(cmd, "knn_rho_delta_site")) {
-        if (nrhs < 11) mexErrMsgTxt("knn_rho_delta_site: F, q0, nq, roff, rs, rn, q_base, n_out, knn, mode [, R]");
+        if (nrhs < 11)
+            mexErrMsgTxt("knn_rho_delta_site: F, q0, nq, roff, rs, rn, q_base, n_out, knn, mode [, R [, site_rows, "
+                         "site_dims]]");
         const mxGPUArray *F = gin(prhs[1]);
         const mwSize *fd = mxGPUGetDimensions(F);
         const int nC = (int)fd[0], nF = (int)(mxGPUGetNumberOfElements(F) / (fd[0] ? fd[0] : 1));
@@ -369,11 +372,30 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
         host_i32(prhs[5], rs, nRuns); host_i32(prhs[6], rn, nRuns);
         const int q_base = (int)mxGetScalar(prhs[7]), n_out = (int)mxGetScalar(prhs[8]);
         const int knn = (int)mxGetScalar(prhs[9]), mode = (int)mxGetScalar(prhs[10]);
-        const mxGPUArray *R = nrhs > 11 ? gin(prhs[11]) : NULL;
+        /* R may be [] to keep the rho computed here */
+        const mxGPUArray *R = nrhs > 11 && mxGetNumberOfElements(prhs[11]) ? gin(prhs[11]) : NULL;
         irc_plan *plan = NULL;
         rc = irc_plan_create(&plan, q0, nq, roff, rs, rn, nCh, q_base, n_out, nF);
         mxFree(q0); mxFree(nq); mxFree(roff); mxFree(rs); mxFree(rn);
         if (rc != IRC_OK) fail(rc, cmd);
+        if (nrhs > 13) {
+            /* stacked sites: int32 row starts (nSites + 1, 0-based, last = nF) and
+             * widths; features past a site's width are zero (irc_plan_set_site_dims) */
+            const int nSites = (int)mxGetNumberOfElements(prhs[13]);
+            if ((int)mxGetNumberOfElements(prhs[12]) != nSites + 1) {
+                irc_plan_destroy(plan);
+                mexErrMsgIdAndTxt("ircgb300:shape", "knn_rho_delta_site: site_rows needs one more entry than site_dims");
+            }
+            int32_t *r32 = (int32_t *)mxMalloc(sizeof(int32_t) * (nSites + 1));
+            int64_t *rows = (int64_t *)mxMalloc(sizeof(int64_t) * (nSites + 1));
+            int32_t *dims = (int32_t *)mxMalloc(sizeof(int32_t) * (nSites ? nSites : 1));
+            host_i32(prhs[12], r32, nSites + 1);
+            host_i32(prhs[13], dims, nSites);
+            for (int k = 0; k <= nSites; ++k) rows[k] = r32[k];
+            rc = irc_plan_set_site_dims(plan, nSites, rows, dims);
+            mxFree(r32); mxFree(rows); mxFree(dims);
+            if (rc != IRC_OK) { irc_plan_destroy(plan); fail(rc, cmd); }
+        }
         mxGPUArray *vr = gout(n_out, 1, mxSINGLE_CLASS), *rho = gout(n_out, 1, mxSINGLE_CLASS),
                    *mi = gout(knn, n_out, mxINT32_CLASS), *de = gout(n_out, 1, mxSINGLE_CLASS),
                    *nn = gout(n_out, 1, mxINT32_CLASS);
