@@ -31,7 +31,8 @@
 //   pass 1  every thread folds its columns into 32 per-column minima (the two
 //           tiles of a wide unit with one three-input min); per query, the
 //           r-th smallest of the 128 minima (r = 48 for BF16, 64 for FP8; a
-//           bitwise search, rounded up by < 2^-11 relative) is an upper bound
+//           bitwise search, rounded up by < 2^-11 relative, < 2^-7 for
+//           slots of at most 16 tiles) is an upper bound
 //           tau on the r-th nearest approximate distance (r distinct
 //           candidates lie at or below it, against knn <= 32);
 //   pass 2  the candidates at or below tau are appended to the query's list
@@ -719,9 +720,12 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
             // The warp's 8 rows at once (independent chains): a bitwise
             // search, from the top, of the largest t with fewer than rank
             // minima below it, i.e. of the rank-th smallest minimum, on the
-            // non-negative float bit patterns.  It stops at TAU_LOW_BIT and
+            // non-negative float bit patterns.  It stops at bit lowb and
             // rounds up, so tau is an upper bound of the rank-th smallest
-            // within 2^-11 of it (a few more candidates listed, never fewer).
+            // within 2^-(lowb - 1) relative of it (a few more candidates
+            // listed, never fewer).  The search is a fixed cost per item,
+            // the extra candidates a cost per tile: slots of at most 16
+            // tiles stop 4 bits earlier (2^-7), longer ones search to 2^-11.
             constexpr int RL = 32 / PARTS;
             unsigned v4[RL][4], ans[RL];
 #pragma unroll
@@ -731,8 +735,9 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
                 for (int u = 0; u < 4; ++u) v4[L][u] = __float_as_uint(bl[u * 32 + lane]);
                 ans[L] = 0u;
             }
+            const int lowb = nts <= 16 ? TAU_LOW_BIT + 4 : TAU_LOW_BIT;   // uniform over the slot
 #pragma unroll 1
-            for (int b = 30; b >= TAU_LOW_BIT; --b) {
+            for (int b = 30; b >= lowb; --b) {
 #pragma unroll
                 for (int L = 0; L < RL; ++L) {
                     const unsigned t = ans[L] | (1u << b);
@@ -747,7 +752,7 @@ __device__ __forceinline__ void epilogue(const irc::PlanDev &p, const irc_tc::Tc
                 for (int L = 1; L < RL; ++L)
                     if (lane == L) a = ans[L];
                 sh.sTau[quarter * 32 + part * RL + lane] =
-                    __uint_as_float(min(a | ((1u << TAU_LOW_BIT) - 1u), 0x7f800000u));
+                    __uint_as_float(min(a | ((1u << lowb) - 1u), 0x7f800000u));
             }
             slot_barrier(s, slot_threads);        // minima rows are read; the list rows may be written
         }
