@@ -18,16 +18,17 @@
 // one MMA per 32 bytes -- make every accumulator the approximate squared
 // distance (FP8: a fixed positive multiple of it).
 //
-// A slot streams its chunk's 128-candidate tiles in units: items of one or
-// two slots use 256-wide units (two tiles, loaded by two TMA boxes into one
-// stage, one N = 256 MMA per K slice, two 256-column accumulators) -- the
-// issue cost of an MMA is the same at N = 256 as at 128, so this halves it
-// per pair -- and four-slot items 128-wide units (four accumulators, one per
-// slot).  Warp roles: warp 0 issues TMA loads (a 3- or 4-stage ring, four
-// 32-row query boxes), warp 1 owns TMEM and issues tcgen05.mma from one
-// thread, warps 2-17 are the epilogue: four per TMEM lane quarter, warp w of
-// a quarter reading columns 32w .. 32w + 31 of every 128-tile.  Each slot's
-// units are streamed twice:
+// A slot streams its chunk's 128-candidate tiles (a per-chunk tile table in
+// the plan) in units: items of one or two slots use 256-wide units (two
+// tiles, loaded by two TMA boxes into one stage, one N = 256 MMA per K slice,
+// two 256-column accumulators) -- the issue cost of an MMA is the same at
+// N = 256 as at 128, so this halves it per pair -- unless the plan asks for
+// 128-wide units (irc_plan_tc_units), and four-slot items 128-wide units
+// (four accumulators, one per slot).  Warp roles: warp 0 claims items and
+// issues TMA loads (a 3- or 4-stage ring, four 32-row query boxes per item),
+// warp 1 owns TMEM and issues tcgen05.mma from one thread, warps 2-17 are the
+// epilogue: four per TMEM lane quarter, warp w of a quarter reading columns
+// 32w .. 32w + 31 of every 128-tile.  Each slot's units are streamed twice:
 //   pass 1  every thread folds its columns into 32 per-column minima (the two
 //           tiles of a wide unit with one three-input min); per query, the
 //           r-th smallest of the 128 minima (r = 48 for BF16, 64 for FP8; a
@@ -36,7 +37,7 @@
 //           tau on the r-th nearest approximate distance (r distinct
 //           candidates lie at or below it, against knn <= 32);
 //   pass 2  the candidates at or below tau are appended to the query's list
-//           in shared memory (~70 per query on random data, at most 192; an
+//           in shared memory (~55-70 per query on random data, at most 192; an
 //           overflowing query is finished by the exact fallback kernel).  In
 //           the BF16 wide units the thresholds are folded into the MMA: each
 //           query's -tau goes into three spare K columns of its operand row,
