@@ -269,6 +269,10 @@ def run_ours(args):
                         "hbm_gbs_at_traffic": (traffic / (tc_ms / 1e3) / 1e9) if traffic else None,
                         "hbm_peak_gbs": peaks["hbm"],
                         "flops_per_pair": 2 * D,
+                        # the MMA work behind it: two passes over K = 16 * ceil((D + 9) / 16) BF16
+                        # values per pair (features, norm and threshold terms), tile padding excluded
+                        "mma_flops_per_pair": 2 * 2 * 16 * ((D + 9 + 15) // 16),
+                        "mma_tflops_issued": 2 * 2 * 16 * ((D + 9 + 15) // 16) * pairs / (tc_ms / 1e3) / 1e12,
                         "peak_src": peaks["src"] + " bf16 burst"}
             else:
                 ach = flops / (dom_ms / 1e3) / 1e12
