@@ -257,6 +257,7 @@ def run_ours(args):
                 # the dominant kernel is the filter, k_knn_tc: its average
                 # launch time over the timed steps (CUDA events on its stream)
                 tc_ms = launch_ms[head]["k_knn_tc"]
+                mma_fpp = 2 * 2 * (32 * ((D + 12 + 31) // 32) if head == "fp8" else 16 * ((D + 9 + 15) // 16))
                 ach = flops / (tc_ms / 1e3) / 1e12
                 # DRAM bytes (read + write) of one launch of k_knn_tc on this
                 # exact workload, captured once with ncu
@@ -269,10 +270,10 @@ def run_ours(args):
                         "hbm_gbs_at_traffic": (traffic / (tc_ms / 1e3) / 1e9) if traffic else None,
                         "hbm_peak_gbs": peaks["hbm"],
                         "flops_per_pair": 2 * D,
-                        # the MMA work behind it: two passes over K = 16 * ceil((D + 9) / 16) BF16
-                        # values per pair (features, norm and threshold terms), tile padding excluded
-                        "mma_flops_per_pair": 2 * 2 * 16 * ((D + 9 + 15) // 16),
-                        "mma_tflops_issued": 2 * 2 * 16 * ((D + 9 + 15) // 16) * pairs / (tc_ms / 1e3) / 1e12,
+                        # the MMA work behind it: two passes over K values per pair (features, norm
+                        # and threshold terms; BF16: 16 per slice, FP8: 32), tile padding excluded
+                        "mma_flops_per_pair": mma_fpp,
+                        "mma_tflops_issued": mma_fpp * pairs / (tc_ms / 1e3) / 1e12,
                         "peak_src": peaks["src"] + " bf16 burst"}
             else:
                 ach = flops / (dom_ms / 1e3) / 1e12
