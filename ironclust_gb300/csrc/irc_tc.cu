@@ -249,17 +249,24 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
             // whole 32-byte sectors: rows are padded to a multiple of 8 floats
             const float *bs = reinterpret_cast<const float *>(Fp + (size_t)idx * Dp4);
             float acc = 0.0f;
+            const int full = nd >> 3, tail = nd & 7;   // whole groups of 8 features, then the rest
 #pragma unroll 2
-            for (int c8 = 0; c8 < (nd + 7) / 8; ++c8) {
+            for (int c8 = 0; c8 < full; ++c8) {
                 float bv[8];
                 ld_nc_v8(bs + 8 * c8, bv);
                 const float4 a0 = qs[2 * c8], a1 = qs[2 * c8 + 1];
                 const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-                const int c = 8 * c8;
-                acc = irc::dterm(acc, bv[0], av[0]);
 #pragma unroll
-                for (int u = 1; u < 8; ++u)
-                    if (c + u < nd) acc = irc::dterm(acc, bv[u], av[u]);
+                for (int u = 0; u < 8; ++u) acc = irc::dterm(acc, bv[u], av[u]);
+            }
+            if (tail) {
+                float bv[8];
+                ld_nc_v8(bs + 8 * full, bv);
+                const float4 a0 = qs[2 * full], a1 = qs[2 * full + 1];
+                const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (u < tail) acc = irc::dterm(acc, bv[u], av[u]);
             }
             if (acc > 0.0f && acc < IRC_SINGLE_INF_F)
                 kv[bi] = ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)idx;
@@ -291,9 +298,27 @@ __device__ __forceinline__ void rerank(const uint32_t *__restrict__ list, int cL
     // more than WARP_KEYS pass, the full sort runs.
     bool sorted = false;
     if (PER >= 2) {
+        // the bits above the highest one in which the keys' distances differ
+        // are common to all of them, hence the answer's: start below them
+        unsigned lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+        for (int i = 0; i < PER; ++i)
+            if (kv[i] != ~0ull) {
+                lo = min(lo, (unsigned)(kv[i] >> 32));
+                hi = max(hi, (unsigned)(kv[i] >> 32));
+            }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
         unsigned ans = 0;
+        int top = 30;
+        if (lo <= hi) {                           // some key: distances are below 2^31 as bit patterns
+            const unsigned x = lo ^ hi;
+            top = x ? 31 - __clz(x) : TAU_LOW_BIT;
+            ans = top < 31 ? lo & ~((2u << top) - 1u) : 0u;
+            top = min(top, 30);
+        }
 #pragma unroll 1
-        for (int b = 30; b >= TAU_LOW_BIT; --b) {
+        for (int b = top; b >= TAU_LOW_BIT; --b) {
             const unsigned t = ans | (1u << b);
             unsigned c = 0;
 #pragma unroll
